@@ -1,0 +1,198 @@
+/* ---------------------------------------------------------------------------
+ * nvector_gb300.h -- NVECTOR_GB300: an N_Vector whose data live in GB300 HBM
+ * and whose every operation is a hand-written sm_103a kernel.
+ *
+ * It is a drop-in for the reference's NVECTOR_CUDA / NVECTOR_SERIAL
+ * constructors: the vector is a standard SUNDIALS N_Vector (ID
+ * SUNDIALS_NVEC_CUSTOM) whose ops table is filled completely, so CVODE, ARKODE,
+ * SPGMR and the Newton solver call it through the generic N_V* dispatch
+ * (sundials_nvector.c:383-835) without any change.
+ *
+ * Replaces (reference interface, file:line):
+ *   N_VNew_Cuda / N_VNewManaged_Cuda / N_VMake_Cuda   nvector_cuda.cu:131-330
+ *   N_VNew_Serial / N_VMake_Serial                    nvector_serial.c:80-215
+ *   N_VCopyToDevice_Cuda / N_VCopyFromDevice_Cuda     nvector_cuda.cu:553-597
+ *   N_VEnableFusedOps_Cuda and the per-op Enable*     nvector_cuda.cu:2089-2260
+ *   every N_V*_Cuda / N_V*_Serial operation           nvector_serial.c:387-1600
+ *
+ * Semantics that differ from NVECTOR_CUDA on purpose:
+ *   - fused and vector-array operations are ENABLED by default;
+ *   - reductions are bitwise deterministic (fixed-order trees, no float
+ *     atomics), so a rerun reproduces every CVODE counter;
+ *   - coefficient / pointer arrays of fused ops travel as kernel parameters
+ *     (no host-to-device staging copy and no extra stream synchronisation);
+ *   - by default products and sums are rounded separately, in the same order
+ *     as NVECTOR_SERIAL, so every streaming and fused op is bit-identical to
+ *     the serial vector; N_VSetFMA_GB300(v, SUNTRUE) selects fused
+ *     multiply-adds instead (one rounding fewer per term).
+ *
+ * Memory: the device array is cudaMalloc'd; a pinned host mirror is created
+ * on first use of N_VGetArrayPointer / N_VCopyFromDevice.  Host <-> device
+ * copies are explicit, as with NVECTOR_CUDA.  All work of a vector and its
+ * clones is ordered on one CUDA stream; a reduction synchronises that stream
+ * only.
+ * ------------------------------------------------------------------------- */
+#ifndef NVECTOR_GB300_H
+#define NVECTOR_GB300_H
+
+#include "sundials_gb300_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- constructors --------------------------------------------------------*/
+
+/* New vector of length `length`; device data allocated, host mirror lazy. */
+SUNGB300_EXPORT N_Vector N_VNew_GB300(sunindextype length, SUNContext sunctx);
+
+/* Same, with all work ordered on the given cudaStream_t (passed as void*). */
+SUNGB300_EXPORT N_Vector N_VNewWithStream_GB300(sunindextype length,
+                                                void* cuda_stream,
+                                                SUNContext sunctx);
+
+/* Vector object with ops and no data (nvector_serial.c:80 N_VNewEmpty_Serial). */
+SUNGB300_EXPORT N_Vector N_VNewEmpty_GB300(SUNContext sunctx);
+
+/* Wrap caller-owned arrays (either may be NULL); nvector_cuda.cu:283 N_VMake_Cuda. */
+SUNGB300_EXPORT N_Vector N_VMake_GB300(sunindextype length, sunrealtype* h_vdata,
+                                       sunrealtype* d_vdata, SUNContext sunctx);
+
+/* ---- data movement and accessors ----------------------------------------*/
+
+SUNGB300_EXPORT void N_VCopyToDevice_GB300(N_Vector v);
+SUNGB300_EXPORT void N_VCopyFromDevice_GB300(N_Vector v);
+SUNGB300_EXPORT sunrealtype* N_VGetHostArrayPointer_GB300(N_Vector v);
+SUNGB300_EXPORT sunrealtype* N_VGetDeviceArrayPointer_GB300(N_Vector v);
+SUNGB300_EXPORT void N_VSetDeviceArrayPointer_GB300(sunrealtype* d_vdata,
+                                                    N_Vector v);
+SUNGB300_EXPORT void* N_VGetStream_GB300(N_Vector v);
+SUNGB300_EXPORT sunbooleantype N_VIsManagedMemory_GB300(N_Vector v);
+
+/* ---- configuration --------------------------------------------------------*/
+
+SUNGB300_EXPORT SUNErrCode N_VEnableFusedOps_GB300(N_Vector v, sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableLinearCombination_GB300(N_Vector v,
+                                                            sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableScaleAddMulti_GB300(N_Vector v,
+                                                        sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableDotProdMulti_GB300(N_Vector v,
+                                                       sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableLinearSumVectorArray_GB300(N_Vector v,
+                                                               sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableScaleVectorArray_GB300(N_Vector v,
+                                                           sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableConstVectorArray_GB300(N_Vector v,
+                                                           sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableWrmsNormVectorArray_GB300(N_Vector v,
+                                                              sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableWrmsNormMaskVectorArray_GB300(N_Vector v,
+                                                                  sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableScaleAddMultiVectorArray_GB300(N_Vector v,
+                                                                   sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableLinearCombinationVectorArray_GB300(
+  N_Vector v, sunbooleantype tf);
+SUNGB300_EXPORT SUNErrCode N_VEnableDotProdMultiLocal_GB300(N_Vector v,
+                                                            sunbooleantype tf);
+
+/* SUNFALSE (default): separately rounded products, NVECTOR_SERIAL order.
+ * SUNTRUE: fused multiply-add.  Inherited by clones. */
+SUNGB300_EXPORT SUNErrCode N_VSetFMA_GB300(N_Vector v, sunbooleantype use_fma);
+
+/* Last CUDA / argument error seen by this library on the calling thread
+ * (0 = none); reading it clears it.  Errors are also reported to the
+ * SUNContext when the library is linked with libsundials_core. */
+SUNGB300_EXPORT int SUNGB300_GetLastError(void);
+SUNGB300_EXPORT const char* SUNGB300_GetLastErrorMessage(void);
+
+/* Number of kernels this library has launched in this process. */
+SUNGB300_EXPORT long long SUNGB300_KernelLaunchCount(void);
+
+/* ---- operations (the ops table entries; same meaning as N_V*_Serial) ----*/
+
+SUNGB300_EXPORT N_Vector_ID N_VGetVectorID_GB300(N_Vector v);
+SUNGB300_EXPORT N_Vector N_VCloneEmpty_GB300(N_Vector w);
+SUNGB300_EXPORT N_Vector N_VClone_GB300(N_Vector w);
+SUNGB300_EXPORT void N_VDestroy_GB300(N_Vector v);
+SUNGB300_EXPORT void N_VSpace_GB300(N_Vector v, sunindextype* lrw,
+                                    sunindextype* liw);
+SUNGB300_EXPORT sunrealtype* N_VGetArrayPointer_GB300(N_Vector v);
+SUNGB300_EXPORT void N_VSetArrayPointer_GB300(sunrealtype* v_data, N_Vector v);
+SUNGB300_EXPORT SUNComm N_VGetCommunicator_GB300(N_Vector v);
+SUNGB300_EXPORT sunindextype N_VGetLength_GB300(N_Vector v);
+
+SUNGB300_EXPORT void N_VLinearSum_GB300(sunrealtype a, N_Vector x, sunrealtype b,
+                                        N_Vector y, N_Vector z);
+SUNGB300_EXPORT void N_VConst_GB300(sunrealtype c, N_Vector z);
+SUNGB300_EXPORT void N_VProd_GB300(N_Vector x, N_Vector y, N_Vector z);
+SUNGB300_EXPORT void N_VDiv_GB300(N_Vector x, N_Vector y, N_Vector z);
+SUNGB300_EXPORT void N_VScale_GB300(sunrealtype c, N_Vector x, N_Vector z);
+SUNGB300_EXPORT void N_VAbs_GB300(N_Vector x, N_Vector z);
+SUNGB300_EXPORT void N_VInv_GB300(N_Vector x, N_Vector z);
+SUNGB300_EXPORT void N_VAddConst_GB300(N_Vector x, sunrealtype b, N_Vector z);
+SUNGB300_EXPORT sunrealtype N_VDotProd_GB300(N_Vector x, N_Vector y);
+SUNGB300_EXPORT sunrealtype N_VMaxNorm_GB300(N_Vector x);
+SUNGB300_EXPORT sunrealtype N_VWrmsNorm_GB300(N_Vector x, N_Vector w);
+SUNGB300_EXPORT sunrealtype N_VWrmsNormMask_GB300(N_Vector x, N_Vector w,
+                                                  N_Vector id);
+SUNGB300_EXPORT sunrealtype N_VMin_GB300(N_Vector x);
+SUNGB300_EXPORT sunrealtype N_VWL2Norm_GB300(N_Vector x, N_Vector w);
+SUNGB300_EXPORT sunrealtype N_VL1Norm_GB300(N_Vector x);
+SUNGB300_EXPORT void N_VCompare_GB300(sunrealtype c, N_Vector x, N_Vector z);
+SUNGB300_EXPORT sunbooleantype N_VInvTest_GB300(N_Vector x, N_Vector z);
+SUNGB300_EXPORT sunbooleantype N_VConstrMask_GB300(N_Vector c, N_Vector x,
+                                                   N_Vector m);
+SUNGB300_EXPORT sunrealtype N_VMinQuotient_GB300(N_Vector num, N_Vector denom);
+
+SUNGB300_EXPORT SUNErrCode N_VLinearCombination_GB300(int nvec, sunrealtype* c,
+                                                      N_Vector* X, N_Vector z);
+SUNGB300_EXPORT SUNErrCode N_VScaleAddMulti_GB300(int nvec, sunrealtype* a,
+                                                  N_Vector x, N_Vector* Y,
+                                                  N_Vector* Z);
+SUNGB300_EXPORT SUNErrCode N_VDotProdMulti_GB300(int nvec, N_Vector x,
+                                                 N_Vector* Y,
+                                                 sunrealtype* dotprods);
+
+SUNGB300_EXPORT SUNErrCode N_VLinearSumVectorArray_GB300(int nvec, sunrealtype a,
+                                                         N_Vector* X,
+                                                         sunrealtype b,
+                                                         N_Vector* Y,
+                                                         N_Vector* Z);
+SUNGB300_EXPORT SUNErrCode N_VScaleVectorArray_GB300(int nvec, sunrealtype* c,
+                                                     N_Vector* X, N_Vector* Z);
+SUNGB300_EXPORT SUNErrCode N_VConstVectorArray_GB300(int nvec, sunrealtype c,
+                                                     N_Vector* Z);
+SUNGB300_EXPORT SUNErrCode N_VWrmsNormVectorArray_GB300(int nvec, N_Vector* X,
+                                                        N_Vector* W,
+                                                        sunrealtype* nrm);
+SUNGB300_EXPORT SUNErrCode N_VWrmsNormMaskVectorArray_GB300(int nvec,
+                                                            N_Vector* X,
+                                                            N_Vector* W,
+                                                            N_Vector id,
+                                                            sunrealtype* nrm);
+SUNGB300_EXPORT SUNErrCode N_VScaleAddMultiVectorArray_GB300(
+  int nvec, int nsum, sunrealtype* a, N_Vector* X, N_Vector** Y, N_Vector** Z);
+SUNGB300_EXPORT SUNErrCode N_VLinearCombinationVectorArray_GB300(
+  int nvec, int nsum, sunrealtype* c, N_Vector** X, N_Vector* Z);
+
+SUNGB300_EXPORT sunrealtype N_VWSqrSumLocal_GB300(N_Vector x, N_Vector w);
+SUNGB300_EXPORT sunrealtype N_VWSqrSumMaskLocal_GB300(N_Vector x, N_Vector w,
+                                                      N_Vector id);
+SUNGB300_EXPORT SUNErrCode N_VDotProdMultiLocal_GB300(int nvec, N_Vector x,
+                                                      N_Vector* Y,
+                                                      sunrealtype* dotprods);
+SUNGB300_EXPORT SUNErrCode N_VDotProdMultiAllReduce_GB300(int nvec, N_Vector x,
+                                                          sunrealtype* sum);
+
+SUNGB300_EXPORT SUNErrCode N_VBufSize_GB300(N_Vector x, sunindextype* size);
+SUNGB300_EXPORT SUNErrCode N_VBufPack_GB300(N_Vector x, void* buf);
+SUNGB300_EXPORT SUNErrCode N_VBufUnpack_GB300(N_Vector x, void* buf);
+
+SUNGB300_EXPORT void N_VPrint_GB300(N_Vector v);
+SUNGB300_EXPORT void N_VPrintFile_GB300(N_Vector v, FILE* outfile);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NVECTOR_GB300_H */

@@ -1,0 +1,89 @@
+"""TEST ORACLE: ctypes access to ``oracle/_build/liboracle.so`` (the C
+restatements of NVECTOR_SERIAL and friends).  Checker only."""
+from __future__ import annotations
+
+import ctypes as ct
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "liboracle.so"
+_lib = None
+
+_P = ct.POINTER(ct.c_double)
+_I = ct.c_int64
+
+
+def lib() -> ct.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from sundials_gb300.build import build_oracle
+            build_oracle()
+        _lib = ct.CDLL(str(LIB_PATH))
+        d = ct.c_double
+        sigs = {
+            "port_linearsum": (None, [d, _P, d, _P, _P, _I]),
+            "port_const": (None, [d, _P, _I]),
+            "port_prod": (None, [_P, _P, _P, _I]),
+            "port_div": (None, [_P, _P, _P, _I]),
+            "port_scale": (None, [d, _P, _P, _I]),
+            "port_abs": (None, [_P, _P, _I]),
+            "port_inv": (None, [_P, _P, _I]),
+            "port_addconst": (None, [_P, d, _P, _I]),
+            "port_compare": (None, [d, _P, _P, _I]),
+            "port_dotprod": (d, [_P, _P, _I]),
+            "port_maxnorm": (d, [_P, _I]),
+            "port_wsqrsum": (d, [_P, _P, _I]),
+            "port_wsqrsummask": (d, [_P, _P, _P, _I]),
+            "port_wrmsnorm": (d, [_P, _P, _I]),
+            "port_wrmsnormmask": (d, [_P, _P, _P, _I]),
+            "port_min": (d, [_P, _I]),
+            "port_wl2norm": (d, [_P, _P, _I]),
+            "port_l1norm": (d, [_P, _I]),
+            "port_invtest": (ct.c_int, [_P, _P, _I]),
+            "port_constrmask": (ct.c_int, [_P, _P, _P, _I]),
+            "port_minquotient": (d, [_P, _P, _I]),
+            "port_linearcombination": (None, [ct.c_int, _P, ct.POINTER(_P), _P, _I]),
+            "port_scaleaddmulti": (None, [ct.c_int, _P, _P, ct.POINTER(_P), ct.POINTER(_P), _I]),
+            "port_dotprodmulti": (None, [ct.c_int, _P, ct.POINTER(_P), _P, _I]),
+        }
+        for name, (res, args) in sigs.items():
+            f = getattr(_lib, name)
+            f.restype = res
+            f.argtypes = args
+    return _lib
+
+
+def ptr(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def ptrs(arrs):
+    arr = (_P * len(arrs))()
+    for i, a in enumerate(arrs):
+        arr[i] = ptr(a)
+    return arr
+
+
+def call(name, *args):
+    return getattr(lib(), name)(*args)
+
+
+def omp():
+    """Multi-core timing variants (same arithmetic, NVECTOR_OPENMP-style sums)."""
+    L = lib()
+    d = ct.c_double
+    for name, res, args in [
+        ("omp_linearsum", None, [d, _P, d, _P, _P, _I]),
+        ("omp_linearcombination", None, [ct.c_int, _P, ct.POINTER(_P), _P, _I]),
+        ("omp_dotprodmulti", None, [ct.c_int, _P, ct.POINTER(_P), _P, _I]),
+        ("omp_wrmsnorm", d, [_P, _P, _I]),
+        ("omp_threads", ct.c_int, []),
+    ]:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
