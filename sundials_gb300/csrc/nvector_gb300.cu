@@ -29,6 +29,7 @@
 
 #include <atomic>
 #include <mutex>
+#include <unordered_map>
 
 #include "../../include/nvector_gb300.h"
 #include "gb300_common.cuh"
@@ -138,26 +139,13 @@ bool ok_or_report(N_Vector v, cudaError_t err, const char* what)
   return false;
 }
 
-Workspace* ws_create(cudaStream_t stream)
+Workspace* ws_alloc(cudaStream_t stream)
 {
   Workspace* ws = (Workspace*)calloc(1, sizeof(Workspace));
   if (!ws) return nullptr;
-  ws->refs = 1;
-  if (stream)
-  {
-    ws->stream     = stream;
-    ws->own_stream = false;
-  }
-  else
-  {
-    if (!check_cuda(cudaStreamCreateWithFlags(&ws->stream, cudaStreamNonBlocking),
-                    "cudaStreamCreate"))
-    {
-      free(ws);
-      return nullptr;
-    }
-    ws->own_stream = true;
-  }
+  ws->refs       = 1;
+  ws->stream     = stream;
+  ws->own_stream = false;
   bool ok = check_cuda(cudaMalloc(&ws->d_partials, sizeof(double) * kMaxRedBlocks * kRowsMax),
                        "cudaMalloc(partials)") &&
             check_cuda(cudaMalloc(&ws->d_counter, sizeof(unsigned int)), "cudaMalloc(counter)") &&
@@ -167,13 +155,43 @@ Workspace* ws_create(cudaStream_t stream)
                        "cudaHostAlloc(result)") &&
             check_cuda(cudaHostGetDevicePointer(&ws->d_result, ws->h_result, 0),
                        "cudaHostGetDevicePointer");
-  if (!ok) return nullptr;
+  if (!ok)
+  {
+    free(ws);
+    return nullptr;
+  }
+  return ws;
+}
+
+// All vectors on one CUDA stream share one workspace.  Vectors created without
+// an explicit stream use the legacy default stream (NVECTOR_CUDA's default
+// policy), so operations on independently created vectors are ordered with
+// each other.  All vectors passed to one operation must live on one stream.
+std::mutex g_ws_mutex;
+std::unordered_map<cudaStream_t, Workspace*> g_ws_by_stream;
+
+Workspace* ws_create(cudaStream_t stream)
+{
+  std::lock_guard<std::mutex> lock(g_ws_mutex);
+  auto it = g_ws_by_stream.find(stream);
+  if (it != g_ws_by_stream.end())
+  {
+    it->second->refs++;
+    return it->second;
+  }
+  Workspace* ws = ws_alloc(stream);
+  if (ws) g_ws_by_stream[stream] = ws;
   return ws;
 }
 
 void ws_release(Workspace* ws)
 {
-  if (!ws || --ws->refs > 0) return;
+  if (!ws) return;
+  {
+    std::lock_guard<std::mutex> lock(g_ws_mutex);
+    if (--ws->refs > 0) return;
+    g_ws_by_stream.erase(ws->stream);
+  }
   cudaStreamSynchronize(ws->stream);
   cudaFree(ws->d_partials);
   cudaFree(ws->d_counter);
@@ -1157,7 +1175,10 @@ N_Vector N_VCloneEmpty_GB300(N_Vector w)
     free_vector(v);
     return nullptr;
   }
-  C(w)->ws->refs++;
+  {
+    std::lock_guard<std::mutex> lock(g_ws_mutex);
+    C(w)->ws->refs++;
+  }
   v->content = c;
   return v;
 }
