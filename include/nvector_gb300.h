@@ -21,10 +21,12 @@
  *     atomics), so a rerun reproduces every CVODE counter;
  *   - coefficient / pointer arrays of fused ops travel as kernel parameters
  *     (no host-to-device staging copy and no extra stream synchronisation);
- *   - by default products and sums are rounded separately, in the same order
- *     as NVECTOR_SERIAL, so every streaming and fused op is bit-identical to
- *     the serial vector; N_VSetFMA_GB300(v, SUNTRUE) selects fused
- *     multiply-adds instead (one rounding fewer per term).
+ *   - arithmetic: by default a*x+y terms are fused multiply-adds, as in the
+ *     reference's NVECTOR_CUDA kernels compiled by nvcc (at most one rounding
+ *     per term away from NVECTOR_SERIAL); N_VSetFMA_GB300(v, SUNFALSE)
+ *     selects separately rounded products and sums in NVECTOR_SERIAL's order,
+ *     which makes every streaming and fused op bit-identical to the serial
+ *     vector (and costs up to 1.8x more FP64 instructions on GB300).
  *
  * Memory: the device array is cudaMalloc'd; a pinned host mirror is created
  * on first use of N_VGetArrayPointer / N_VCopyFromDevice.  Host <-> device
@@ -95,8 +97,9 @@ SUNGB300_EXPORT SUNErrCode N_VEnableLinearCombinationVectorArray_GB300(
 SUNGB300_EXPORT SUNErrCode N_VEnableDotProdMultiLocal_GB300(N_Vector v,
                                                             sunbooleantype tf);
 
-/* SUNFALSE (default): separately rounded products, NVECTOR_SERIAL order.
- * SUNTRUE: fused multiply-add.  Inherited by clones. */
+/* SUNTRUE (default): fused multiply-add.  SUNFALSE: separately rounded
+ * products and sums in NVECTOR_SERIAL's order.  Inherited by clones; an
+ * operation uses the mode of its output vector (of x for reductions). */
 SUNGB300_EXPORT SUNErrCode N_VSetFMA_GB300(N_Vector v, sunbooleantype use_fma);
 
 /* Last CUDA / argument error seen by this library on the calling thread

@@ -87,3 +87,30 @@ def omp():
         f.restype = res
         f.argtypes = args
     return L
+
+
+def bdf_batch(batch, rtol=1e-6, atol=1e-12, tout=100.0, mxstep=1000000, threads=0,
+              first=0, count=None):
+    """Run the CVODE restatement over systems [first, first+count) of a
+    KineticsBatch; returns (stats structured array, yout flat array)."""
+    from sundials_gb300.kinetics import STATS_DTYPE
+    L = lib()
+    if count is None:
+        count = batch.nsys - first
+    f = L.bdf_port_batch
+    i32 = ct.POINTER(ct.c_int32)
+    i64 = ct.POINTER(ct.c_int64)
+    f.restype = None
+    f.argtypes = [ct.c_int64, ct.c_int64, i32, i64, i64, i32, i32, i32, i32, _P, _P,
+                  ct.c_double, ct.c_double, ct.c_double, ct.c_long, ct.c_int, _P, ct.c_void_p]
+    c = lambda a, t: np.ascontiguousarray(a, dtype=t)
+    n, yo, ro = c(batch.n, np.int32), c(batch.y_off, np.int64), c(batch.r_off, np.int64)
+    rt, ra, rb, rc = (c(a, np.int32) for a in (batch.rtype, batch.ra, batch.rb, batch.rc))
+    rk, y0 = c(batch.rk, np.float64), c(batch.y0, np.float64)
+    yout = np.zeros_like(y0)
+    stats = np.zeros(count, STATS_DTYPE)
+    f(first, count, n.ctypes.data_as(i32), yo.ctypes.data_as(i64), ro.ctypes.data_as(i64),
+      rt.ctypes.data_as(i32), ra.ctypes.data_as(i32), rb.ctypes.data_as(i32),
+      rc.ctypes.data_as(i32), rk.ctypes.data_as(_P), y0.ctypes.data_as(_P), rtol, atol, tout,
+      mxstep, threads, yout.ctypes.data_as(_P), stats.ctypes.data)
+    return stats, yout

@@ -83,7 +83,7 @@ def build_library(verbose: bool = False) -> Path:
 
 
 def build_oracle(verbose: bool = False) -> Path:
-    srcs = sorted(ORACLE.glob("*.c"))
+    srcs = sorted(ORACLE.glob("*_port.c"))
     out = ORACLE_LIB
     out.parent.mkdir(parents=True, exist_ok=True)
     if _stale(out, srcs + list(ORACLE.glob("*.h"))):

@@ -3,9 +3,12 @@
 //
 // Operation semantics follow NVECTOR_SERIAL (src/nvector/serial/
 // nvector_serial.c:387-1600): the same special cases of LinearSum (a==b ->
-// a*(x+y), a==-b -> a*(x-y)), the same element order of fused sums, and in
-// the default arithmetic mode the same rounding of every product and sum, so
-// streaming and fused operations give the serial vector's bits.
+// a*(x+y), a==-b -> a*(x-y)) and the same element order of fused sums.  Two
+// arithmetic modes: FMA (default; what nvcc makes of NVECTOR_CUDA's kernels)
+// and EXACT (every product and sum rounded separately, giving the serial
+// vector's bits).  On GB300 the FP64 pipe (~1.2 TFLOP/s) rather than HBM
+// bounds most of these operations, so the mode also sets their speed: FMA
+// issues 5 instead of 9 FP64 instructions per element of LinearCombination(5).
 //
 // Kernel design (GB300-first, not a port of NVECTOR_CUDA's kernels):
 //  * element pairs move as 16-byte double2 loads/stores when every operand
@@ -947,7 +950,7 @@ N_Vector make_vector(sunindextype length, cudaStream_t stream, SUNContext sunctx
   N_Vector v = new_empty(sunctx);
   if (!v) return nullptr;
   Workspace* ws = ws_create(stream);
-  Content* c    = ws ? new_content(length, ws, false) : nullptr;
+  Content* c    = ws ? new_content(length, ws, true) : nullptr;
   if (!c || (alloc && !alloc_device(c)))
   {
     if (c) free(c);

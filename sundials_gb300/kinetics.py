@@ -133,3 +133,36 @@ def rhs(batch: KineticsBatch, i: int, y: np.ndarray) -> np.ndarray:
             f[B] = f[B] - rate
             f[Cc] = f[Cc] + rate
     return f
+
+
+# ------------------------------------------------------------- file format
+STATS_FIELDS = ["nst", "nfe", "nsetups", "nje", "nni", "ncfn", "netf", "nnf", "flag", "qu"]
+STATS_DTYPE = np.dtype([(f, "<i8") for f in STATS_FIELDS] + [("tn", "<f8"), ("hu", "<f8")])
+
+
+def write_bin(batch: KineticsBatch, path) -> None:
+    """Problem file read by the C drivers (layout in oracle/kinetics_model.h)."""
+    with open(path, "wb") as f:
+        np.array([batch.nsys, batch.y0.size, batch.rk.size], "<i8").tofile(f)
+        batch.n.astype("<i4").tofile(f)
+        batch.y_off.astype("<i8").tofile(f)
+        batch.r_off.astype("<i8").tofile(f)
+        for a in (batch.rtype, batch.ra, batch.rb, batch.rc):
+            a.astype("<i4").tofile(f)
+        batch.rk.astype("<f8").tofile(f)
+        batch.y0.astype("<f8").tofile(f)
+
+
+def read_results(path, batch: KineticsBatch):
+    """(stats structured array, y list) from a driver's output file."""
+    raw = open(path, "rb").read()
+    stats = np.zeros(batch.nsys, STATS_DTYPE)
+    ys = []
+    off = 0
+    for i in range(batch.nsys):
+        stats[i] = np.frombuffer(raw, STATS_DTYPE, 1, off)[0]
+        off += STATS_DTYPE.itemsize
+        n = int(batch.n[i])
+        ys.append(np.frombuffer(raw, "<f8", n, off).copy())
+        off += 8 * n
+    return stats, ys

@@ -3,8 +3,9 @@
 Every operation is called through the vector's ops table, as CVODE does.
 Tolerances:
   * elementwise, fused (LinearCombination, ScaleAddMulti) and vector-array
-    operations: BIT-EXACT in the default arithmetic mode (separately rounded
-    products, serial term order);
+    operations: BIT-EXACT in the serial-order arithmetic mode
+    (N_VSetFMA_GB300(v, 0)); in the default FMA mode within one rounding per
+    term: |gpu - serial| <= 2.3e-16 * sum_k |c_k x_k|;
   * max / min reductions (MaxNorm, Min, MinQuotient, InvTest, ConstrMask):
     bit-exact (order-free);
   * sum reductions (DotProd, WrmsNorm, WL2Norm, L1Norm, DotProdMulti):
@@ -36,8 +37,11 @@ def rnd(n, seed, lo=-1.0, hi=1.0):
     return np.random.default_rng(seed).uniform(lo, hi, n)
 
 
-def nv(a):
-    return NVector.from_numpy(a)
+def nv(a, exact=True):
+    """Vectors of the bit-exact tests use the serial-order arithmetic mode."""
+    v = NVector.from_numpy(a)
+    v.set_fma(not exact)
+    return v
 
 
 def bits_equal(a, b):
@@ -322,10 +326,12 @@ def test_unaligned_operands_take_scalar_path(gb300_lib, port):
     lib = gb300_lib
     n = 10001
     base = NVector(n + 1)
+    base.set_fma(False)
     x = rnd(n, 600)
     base.set(np.concatenate([[0.0], x]))
     view = lib.N_VMake_GB300(n, None, ct.cast(base.device_ptr + 8, _lib.P_real), None)
     V = NVector(n, handle=view)
+    V.set_fma(False)
     Y = nv(rnd(n, 601))
     Z = Y.clone()
     V.ops["nvlinearsum"](0.3, V.v, 0.7, Y.v, Z.v)
@@ -372,18 +378,34 @@ def test_fused_ops_can_be_disabled(gb300_lib):
     assert c.ops["nvdotprodmulti"] is None
 
 
-def test_fma_mode_close_to_exact(gb300_lib, port):
+def test_fma_mode_within_one_rounding_per_term(gb300_lib, port):
     n = 100003
     x, y = rnd(n, 700), rnd(n, 701)
-    X, Y = nv(x), nv(y)
+    X, Y = nv(x, exact=False), nv(y, exact=False)
     Z = X.clone()
-    X.set_fma(True)
-    Z.set_fma(True)
     Z.ops["nvlinearsum"](0.3, X.v, 0.7, Y.v, Z.v)
     ref = np.empty(n)
     port.call("port_linearsum", 0.3, port.ptr(x), 0.7, port.ptr(y), port.ptr(ref), n)
     err = np.abs(Z.get() - ref)
     assert np.all(err <= 2.3e-16 * (np.abs(0.3 * x) + np.abs(0.7 * y)))
+    # LinearCombination(5) and ScaleAddMulti(3) in the default FMA mode
+    xs = [rnd(n, 710 + k) for k in range(5)]
+    c = rnd(5, 720)
+    Xs = [nv(a, exact=False) for a in xs]
+    Zc = nv(np.zeros(n), exact=False)
+    Zc.ops["nvlinearcombination"](5, _lib.real_array(c), _lib.nv_array([v.v for v in Xs]), Zc.v)
+    port.call("port_linearcombination", 5, port.ptr(c), port.ptrs(xs), port.ptr(ref), n)
+    bound = 2.3e-16 * 5 * sum(np.abs(c[k] * xs[k]) for k in range(5))
+    assert np.all(np.abs(Zc.get() - ref) <= bound)
+    Zs = [nv(np.zeros(n), exact=False) for _ in range(3)]
+    X.ops["nvscaleaddmulti"](3, _lib.real_array(c[:3]), X.v, _lib.nv_array([v.v for v in Xs[:3]]),
+                             _lib.nv_array([v.v for v in Zs]))
+    for k in range(3):
+        exact = c[k] * x + xs[k]
+        assert np.all(np.abs(Zs[k].get() - exact) <= 2.3e-16 * (np.abs(c[k] * x) + np.abs(xs[k])))
+    # reductions in FMA mode stay within the sum tolerance
+    g = X.ops["nvdotprod"](X.v, Y.v)
+    assert sum_close(g, port.call("port_dotprod", port.ptr(x), port.ptr(y), n), x * y)
 
 
 def test_identity_and_utilities(gb300_lib):
