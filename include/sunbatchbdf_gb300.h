@@ -1,0 +1,118 @@
+/* ---------------------------------------------------------------------------
+ * sunbatchbdf_gb300.h -- SUNBatchBDF_GB300: thousands of independent stiff
+ * systems of uneven size integrated by CVODE's BDF method in ONE persistent
+ * GPU launch, each system with its own step size, order and counters.
+ *
+ * The reference has no per-system step control: one CVODE instance owns one
+ * h, q and set of counters for its whole N_Vector (src/cvode/cvode_impl.h,
+ * cv_h / cv_q), and its batched examples step all systems together
+ * (examples/cvode/cuda/cvRoberts_block_cusolversp_batchqr.cu:196-223).  The
+ * semantics here are therefore those of one independent CVode(tout,
+ * CV_NORMAL) call per system with NVECTOR_SERIAL, SUNLINSOL_DENSE and an
+ * analytic Jacobian (src/cvode/cvode.c:1037-3727, cvode_nls.c, cvode_ls.c,
+ * sunnonlinsol_newton.c, sundials_dense.c), restated on the device.  The
+ * per-system counters have the meaning of CVodeGetNumSteps, GetNumRhsEvals,
+ * GetNumLinSolvSetups, GetNumJacEvals, GetNumNonlinSolvIters,
+ * GetNumStepSolveFails, GetNumErrTestFails, GetNumNonlinSolvConvFails,
+ * GetLastOrder, GetCurrentTime and GetLastStep (src/cvode/cvode_io.c:1053-1626).
+ *
+ * The right-hand side is a mass-action reaction network given as data
+ * (A -> B and A + B -> C reactions with rate constants), evaluated and
+ * differentiated on the device.  This entry point has no counterpart in the
+ * reference's plugin API (no reference plugin point exists for per-system
+ * step control); its problem layout is documented below.
+ *
+ * Arithmetic modes (SUNBatchBDF_GB300_SetMode):
+ *   SUNBATCHBDF_FP64        FP64 throughout, fused multiply-adds (default);
+ *   SUNBATCHBDF_FP64_EXACT  FP64 with every product and sum rounded
+ *                           separately and sums in CVODE's sequential order,
+ *                           i.e. the reference's arithmetic on x86-64 (only
+ *                           pow() may differ by an ulp);
+ *   SUNBATCHBDF_MIXED       Newton matrix I - gamma*J factored and solved in
+ *                           FP32, each solve followed by FP64 iterative
+ *                           refinement (residual with the FP64 Jacobian);
+ *                           residuals, norms, error test and step control FP64.
+ * ------------------------------------------------------------------------- */
+#ifndef SUNBATCHBDF_GB300_H
+#define SUNBATCHBDF_GB300_H
+
+#include <stdint.h>
+
+#include "sundials_gb300_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SUNBATCHBDF_FP64       0
+#define SUNBATCHBDF_FP64_EXACT 1
+#define SUNBATCHBDF_MIXED      2
+
+#define SUNBATCHBDF_NMAX 64 /* largest system size */
+
+/* Mass-action problem.  All arrays are HOST arrays; reaction r of system s
+ * is r_off[s] <= r < r_off[s+1], species indices are local (0..n[s]-1):
+ *   rtype[r] == 0:  ra -> rb,        rate = rk * y[ra]
+ *   rtype[r] == 1:  ra + rb -> rc,   rate = (rk * y[ra]) * y[rb]
+ * f sums the signed rates of the reactions in index order (see
+ * sundials_gb300/kinetics.py for the definition of every summation order). */
+typedef struct
+{
+  int64_t nsys;
+  const int32_t* n;     /* [nsys]   species per system, 1..64 */
+  const int64_t* y_off; /* [nsys+1] offsets of each system's state */
+  const int64_t* r_off; /* [nsys+1] offsets of each system's reactions */
+  const int32_t* rtype; /* [R] */
+  const int32_t* ra;    /* [R] */
+  const int32_t* rb;    /* [R] */
+  const int32_t* rc;    /* [R] (-1 for A -> B) */
+  const double* rk;     /* [R] */
+} SUNBatchBDFProblem;
+
+/* Per-system result record (same layout as the CPU oracle's KinStats). */
+typedef struct
+{
+  int64_t nst, nfe, nsetups, nje, nni, ncfn, netf, nnf;
+  int64_t flag; /* CVode return value: 0 success, <0 failure */
+  int64_t qu;   /* last order used */
+  double tn;    /* internal time reached */
+  double hu;    /* last step size used */
+} SUNBatchBDFStats;
+
+typedef struct SUNBatchBDF_GB300_* SUNBatchBDF_GB300;
+
+/* Copies the problem to the device; stream = cudaStream_t (NULL: default). */
+SUNGB300_EXPORT SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob,
+                                                           void* cuda_stream);
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetTolerances(SUNBatchBDF_GB300 b, double rtol,
+                                                    double atol);
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetMaxNumSteps(SUNBatchBDF_GB300 b, long mxstep);
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetMode(SUNBatchBDF_GB300 b, int mode);
+/* Refinement sweeps after each FP32 solve in SUNBATCHBDF_MIXED (default 1). */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetRefinementSweeps(SUNBatchBDF_GB300 b, int sweeps);
+
+/* Integrate every system from t0 to tout (one CVode(tout, CV_NORMAL) each).
+ * y0 / yout: Sum(n) doubles; host or device pointers (cudaMemcpyDefault
+ * semantics).  stats: nsys records (host or device) or NULL.  Returns 0 when
+ * the launch succeeded (per-system failures are in stats[s].flag), a
+ * SUN_ERR_* code otherwise. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_Solve(SUNBatchBDF_GB300 b, double t0, const double* y0,
+                                            double tout, double* yout,
+                                            SUNBatchBDFStats* stats);
+
+/* Same as Solve with device pointers only, no synchronisation: enqueued on
+ * the object's stream (may be captured into a CUDA graph). */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0,
+                                                 const double* d_y0, double tout,
+                                                 double* d_yout, SUNBatchBDFStats* d_stats);
+
+/* Wall time of the last Solve's integration kernel in milliseconds. */
+SUNGB300_EXPORT double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b);
+
+SUNGB300_EXPORT void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUNBATCHBDF_GB300_H */

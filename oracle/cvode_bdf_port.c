@@ -33,6 +33,14 @@
 #include <omp.h>
 
 #include "kinetics_model.h"
+#include "../sundials_gb300/csrc/ddpow.h"
+
+/* Which pow() the step-size controller uses: 0 = the C library's (what the
+ * reference calls through SUNRpowerR), 1 = the correctly rounded
+ * double-double pow that the GPU integrator's exact mode uses. */
+static int g_pow_dd = 0;
+void bdf_port_set_pow(int dd) { g_pow_dd = dd; }
+static inline double cv_pow(double x, double y) { return g_pow_dd ? dd_pow(x, y) : pow(x, y); }
 
 #define NMAX 64
 #define QMAX 5
@@ -518,7 +526,7 @@ static int do_error_test(Bdf* m, int* nflagPtr, double saved_t, int* nefPtr, dou
   m->etamax = 1.0;
   if (*nefPtr <= MXNEF1)
   {
-    m->eta = 1.0 / (pow(BIAS2 * dsm, 1.0 / m->L) + ADDON);
+    m->eta = 1.0 / (cv_pow(BIAS2 * dsm, 1.0 / m->L) + ADDON);
     double lo = 0.0; /* hmin/|h| */
     m->eta    = ETA_MIN_EF > (m->eta > lo ? m->eta : lo) ? ETA_MIN_EF : (m->eta > lo ? m->eta : lo);
     if (*nefPtr >= SMALL_NEF) m->eta = m->eta < ETA_MAX_EF ? m->eta : ETA_MAX_EF;
@@ -596,7 +604,7 @@ static double compute_etaqm1(Bdf* m)
   if (m->q > 1)
   {
     double ddn = wrms(m, m->zn[m->q]) * m->tq[1];
-    m->etaqm1  = 1.0 / (pow(BIAS1 * ddn, 1.0 / m->q) + ADDON);
+    m->etaqm1  = 1.0 / (cv_pow(BIAS1 * ddn, 1.0 / m->q) + ADDON);
   }
   return m->etaqm1;
 }
@@ -613,7 +621,7 @@ static double compute_etaqp1(Bdf* m)
     const double a = -cquot;
     for (int i = 0; i < m->n; i++) m->tempv[i] = (a * m->zn[QMAX][i]) + m->acor[i];
     double dup = wrms(m, m->tempv) * m->tq[3];
-    m->etaqp1  = 1.0 / (pow(BIAS3 * dup, 1.0 / (m->L + 1)) + ADDON);
+    m->etaqp1  = 1.0 / (cv_pow(BIAS3 * dup, 1.0 / (m->L + 1)) + ADDON);
   }
   return m->etaqp1;
 }
@@ -656,7 +664,7 @@ static void prepare_next_step(Bdf* m, double dsm)
     m->eta    = 1.0;
     return;
   }
-  m->etaq = 1.0 / (pow(BIAS2 * dsm, 1.0 / m->L) + ADDON);
+  m->etaq = 1.0 / (cv_pow(BIAS2 * dsm, 1.0 / m->L) + ADDON);
   if (m->qwait != 0)
   {
     m->eta    = m->etaq;

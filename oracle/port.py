@@ -90,11 +90,14 @@ def omp():
 
 
 def bdf_batch(batch, rtol=1e-6, atol=1e-12, tout=100.0, mxstep=1000000, threads=0,
-              first=0, count=None):
+              first=0, count=None, dd_pow=False):
     """Run the CVODE restatement over systems [first, first+count) of a
-    KineticsBatch; returns (stats structured array, yout flat array)."""
+    KineticsBatch; returns (stats structured array, yout flat array).
+    dd_pow=True swaps the C library's pow for the correctly rounded one."""
     from sundials_gb300.kinetics import STATS_DTYPE
     L = lib()
+    L.bdf_port_set_pow.argtypes = [ct.c_int]
+    L.bdf_port_set_pow(1 if dd_pow else 0)
     if count is None:
         count = batch.nsys - first
     f = L.bdf_port_batch
@@ -113,4 +116,5 @@ def bdf_batch(batch, rtol=1e-6, atol=1e-12, tout=100.0, mxstep=1000000, threads=
       rt.ctypes.data_as(i32), ra.ctypes.data_as(i32), rb.ctypes.data_as(i32),
       rc.ctypes.data_as(i32), rk.ctypes.data_as(_P), y0.ctypes.data_as(_P), rtol, atol, tout,
       mxstep, threads, yout.ctypes.data_as(_P), stats.ctypes.data)
+    L.bdf_port_set_pow(0)
     return stats, yout

@@ -1,0 +1,97 @@
+"""Host-side handle for SUNBatchBDF_GB300 (include/sunbatchbdf_gb300.h)."""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+from .kinetics import STATS_DTYPE, KineticsBatch
+
+FP64, FP64_EXACT, MIXED = 0, 1, 2
+MODES = {"fp64": FP64, "fp64_exact": FP64_EXACT, "mixed": MIXED}
+
+
+class _Problem(ct.Structure):
+    _fields_ = [("nsys", ct.c_int64)] + [
+        (name, ct.c_void_p) for name in ("n", "y_off", "r_off", "rtype", "ra", "rb", "rc", "rk")]
+
+
+def _declare(lib):
+    if getattr(lib, "_batch_declared", False):
+        return
+    vp = ct.c_void_p
+    for name, res, args in [
+        ("SUNBatchBDF_GB300_Create", vp, [ct.POINTER(_Problem), vp]),
+        ("SUNBatchBDF_GB300_SetTolerances", ct.c_int, [vp, ct.c_double, ct.c_double]),
+        ("SUNBatchBDF_GB300_SetMaxNumSteps", ct.c_int, [vp, ct.c_long]),
+        ("SUNBatchBDF_GB300_SetMode", ct.c_int, [vp, ct.c_int]),
+        ("SUNBatchBDF_GB300_SetRefinementSweeps", ct.c_int, [vp, ct.c_int]),
+        ("SUNBatchBDF_GB300_Solve", ct.c_int, [vp, ct.c_double, vp, ct.c_double, vp, vp]),
+        ("SUNBatchBDF_GB300_SolveAsync", ct.c_int, [vp, ct.c_double, vp, ct.c_double, vp, vp]),
+        ("SUNBatchBDF_GB300_LastKernelMs", ct.c_double, [vp]),
+        ("SUNBatchBDF_GB300_Free", None, [vp]),
+    ]:
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    lib._batch_declared = True
+
+
+class BatchBDF:
+    def __init__(self, batch: KineticsBatch, stream=None):
+        self.lib = _lib.load()
+        _declare(self.lib)
+        self.batch = batch
+        self._keep = [np.ascontiguousarray(batch.n, np.int32),
+                      np.ascontiguousarray(batch.y_off, np.int64),
+                      np.ascontiguousarray(batch.r_off, np.int64),
+                      np.ascontiguousarray(batch.rtype, np.int32),
+                      np.ascontiguousarray(batch.ra, np.int32),
+                      np.ascontiguousarray(batch.rb, np.int32),
+                      np.ascontiguousarray(batch.rc, np.int32),
+                      np.ascontiguousarray(batch.rk, np.float64)]
+        prob = _Problem(batch.nsys, *[a.ctypes.data for a in self._keep])
+        self.h = self.lib.SUNBatchBDF_GB300_Create(ct.byref(prob), stream)
+        if not self.h:
+            raise RuntimeError("SUNBatchBDF_GB300_Create failed: "
+                               + self.lib.SUNGB300_GetLastErrorMessage().decode())
+
+    def configure(self, rtol=1e-6, atol=1e-12, mode="fp64", mxstep=1000000, refine=1):
+        L = self.lib
+        assert L.SUNBatchBDF_GB300_SetTolerances(self.h, rtol, atol) == 0
+        assert L.SUNBatchBDF_GB300_SetMode(self.h, MODES[mode] if isinstance(mode, str) else mode) == 0
+        assert L.SUNBatchBDF_GB300_SetMaxNumSteps(self.h, mxstep) == 0
+        assert L.SUNBatchBDF_GB300_SetRefinementSweeps(self.h, refine) == 0
+        return self
+
+    def solve(self, tout=100.0, t0=0.0, y0=None):
+        y0 = np.ascontiguousarray(self.batch.y0 if y0 is None else y0, np.float64)
+        yout = np.zeros_like(y0)
+        stats = np.zeros(self.batch.nsys, STATS_DTYPE)
+        rc = self.lib.SUNBatchBDF_GB300_Solve(self.h, t0, y0.ctypes.data, tout,
+                                              yout.ctypes.data, stats.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"SUNBatchBDF_GB300_Solve failed ({rc}): "
+                               + self.lib.SUNGB300_GetLastErrorMessage().decode())
+        return yout, stats
+
+    def solve_device(self, d_y0: int, d_yout: int, d_stats: int, tout=100.0, t0=0.0):
+        rc = self.lib.SUNBatchBDF_GB300_SolveAsync(self.h, t0, d_y0, tout, d_yout, d_stats)
+        if rc != 0:
+            raise RuntimeError(f"SUNBatchBDF_GB300_SolveAsync failed ({rc})")
+
+    @property
+    def last_kernel_ms(self) -> float:
+        return self.lib.SUNBatchBDF_GB300_LastKernelMs(self.h)
+
+    def free(self):
+        if self.h:
+            self.lib.SUNBatchBDF_GB300_Free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass

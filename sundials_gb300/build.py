@@ -39,6 +39,11 @@ NVCC_FLAGS = ARCH + [
 ]
 
 
+# Extra flags per translation unit: the exact-arithmetic batched integrator
+# must not contract products and sums into FMAs.
+PER_FILE_FLAGS = {"batch_bdf_exact.cu": ["-fmad=false"]}
+
+
 def _nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and Path(cand).exists():
@@ -70,7 +75,8 @@ def build_library(verbose: bool = False) -> Path:
     for src in sources:
         obj = OBJ / (src.stem + ".o")
         if _stale(obj, [src] + headers):
-            jobs.append([nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)])
+            jobs.append([nvcc, *NVCC_FLAGS, *PER_FILE_FLAGS.get(src.name, []), "-c", str(src),
+                         "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for fut in [ex.submit(_run, j) for j in jobs]:
             fut.result()

@@ -1,0 +1,328 @@
+// batch_bdf.cu -- host side of SUNBatchBDF_GB300: problem upload, the
+// species/reactant indexes the device right-hand side and Jacobian walk, the
+// processing order, per-warp scratch, and the persistent launch.
+#include <cuda_runtime.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "../../include/sunbatchbdf_gb300.h"
+#include "batch_bdf_kernel.cuh"
+#include "gb300_common.cuh"
+
+namespace bdf {
+cudaError_t launch_fast(const Params& P, int mode, int grid, cudaStream_t stream);
+cudaError_t occupancy_fast(int mode, int* blocks_per_sm);
+cudaError_t launch_exact(const Params& P, int grid, cudaStream_t stream);
+cudaError_t occupancy_exact(int* blocks_per_sm);
+}  // namespace bdf
+
+using namespace bdf;
+
+struct SUNBatchBDF_GB300_
+{
+  cudaStream_t stream;
+  int64_t nsys, Y, R;
+  DevProblem dp;
+  std::vector<void*> allocs;
+  double rtol = 1e-6, atol = 1e-12;
+  long mxstep  = 1000000;
+  int mode     = SUNBATCHBDF_FP64;
+  int refine   = 1;
+  double* d_y0 = nullptr;
+  double* d_yout = nullptr;
+  SUNBatchBDFStats* d_stats = nullptr;
+  unsigned int* d_next = nullptr;
+  double* d_scratch = nullptr;
+  int* d_piv = nullptr;
+  int slots = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0.f;
+};
+
+namespace {
+
+template <class T>
+T* upload(SUNBatchBDF_GB300 b, const T* h, size_t count)
+{
+  T* d = nullptr;
+  if (!gb300::check_cuda(cudaMalloc(&d, sizeof(T) * (count ? count : 1)), "cudaMalloc(batch)"))
+    return nullptr;
+  b->allocs.push_back(d);
+  if (count && !gb300::check_cuda(cudaMemcpy(d, h, sizeof(T) * count, cudaMemcpyHostToDevice),
+                                  "cudaMemcpy(batch)"))
+    return nullptr;
+  return d;
+}
+
+bool is_device_ptr(const void* p)
+{
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess)
+  {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int grid_for(SUNBatchBDF_GB300 b, int mode)
+{
+  int per_sm = 0;
+  cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(&per_sm)
+                                                   : occupancy_fast(mode, &per_sm);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  int grid = gb300::num_sms() * per_sm;
+  int64_t need = (b->nsys + WARPS - 1) / WARPS;
+  if (need < grid) grid = (int)need;
+  return grid < 1 ? 1 : grid;
+}
+
+bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
+{
+  if (slots <= b->slots) return true;
+  if (!gb300::check_cuda(cudaMalloc(&b->d_scratch, sizeof(double) * 2 * NMAX * NMAX * (size_t)slots),
+                         "cudaMalloc(scratch)") ||
+      !gb300::check_cuda(cudaMalloc(&b->d_piv, sizeof(int) * NMAX * (size_t)slots),
+                         "cudaMalloc(pivots)"))
+    return false;
+  b->slots = slots;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void* cuda_stream)
+{
+  if (!prob || prob->nsys <= 0) return nullptr;
+  const int64_t nsys = prob->nsys;
+  for (int64_t s = 0; s < nsys; s++)
+    if (prob->n[s] < 1 || prob->n[s] > NMAX ||
+        prob->r_off[s + 1] - prob->r_off[s] > RMAX)
+    {
+      gb300::set_error(SUN_ERR_ARG_OUTOFRANGE, "system size outside 1..64 or > 128 reactions");
+      return nullptr;
+    }
+  SUNBatchBDF_GB300 b = new SUNBatchBDF_GB300_();
+  b->stream = (cudaStream_t)cuda_stream;
+  b->nsys   = nsys;
+  b->Y      = prob->y_off[nsys];
+  b->R      = prob->r_off[nsys];
+
+  // Species CSR (f) and reactant CSR (J), both in reaction order.
+  std::vector<int32_t> fptr(b->Y + nsys), jptr(b->Y + nsys);
+  std::vector<int64_t> e_off(nsys + 1, 0), je_off(nsys + 1, 0);
+  std::vector<int32_t> fent, jent;
+  fent.reserve(3 * b->R);
+  jent.reserve(2 * b->R);
+  std::vector<std::vector<int32_t>> fl(NMAX), jl(NMAX);
+  for (int64_t s = 0; s < nsys; s++)
+  {
+    const int n = prob->n[s];
+    for (int i = 0; i < n; i++)
+    {
+      fl[i].clear();
+      jl[i].clear();
+    }
+    for (int64_t r = prob->r_off[s]; r < prob->r_off[s + 1]; r++)
+    {
+      const int lr = (int)(r - prob->r_off[s]);
+      const int a = prob->ra[r], bb = prob->rb[r];
+      if (prob->rtype[r] == 0)
+      {
+        fl[a].push_back(lr << 1 | 1);
+        fl[bb].push_back(lr << 1);
+        jl[a].push_back(lr << 1);
+      }
+      else
+      {
+        const int c = prob->rc[r];
+        fl[a].push_back(lr << 1 | 1);
+        fl[bb].push_back(lr << 1 | 1);
+        fl[c].push_back(lr << 1);
+        jl[a].push_back(lr << 1);
+        jl[bb].push_back(lr << 1 | 1);
+      }
+    }
+    const int64_t base = prob->y_off[s] + s;
+    int32_t fo = 0, jo = 0;
+    for (int i = 0; i < n; i++)
+    {
+      fptr[base + i] = fo;
+      jptr[base + i] = jo;
+      fent.insert(fent.end(), fl[i].begin(), fl[i].end());
+      jent.insert(jent.end(), jl[i].begin(), jl[i].end());
+      fo += (int32_t)fl[i].size();
+      jo += (int32_t)jl[i].size();
+    }
+    fptr[base + n] = fo;
+    jptr[base + n] = jo;
+    e_off[s + 1]   = e_off[s] + fo;
+    je_off[s + 1]  = je_off[s] + jo;
+  }
+  // Largest systems first: the cost of a system grows like n^3.
+  std::vector<int32_t> order(nsys);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t x, int32_t y) { return prob->n[x] > prob->n[y]; });
+
+  DevProblem& d = b->dp;
+  d.nsys   = nsys;
+  d.n      = upload(b, prob->n, nsys);
+  d.y_off  = upload(b, prob->y_off, nsys + 1);
+  d.r_off  = upload(b, prob->r_off, nsys + 1);
+  d.rtype  = upload(b, prob->rtype, b->R);
+  d.ra     = upload(b, prob->ra, b->R);
+  d.rb     = upload(b, prob->rb, b->R);
+  d.rc     = upload(b, prob->rc, b->R);
+  d.rk     = upload(b, prob->rk, b->R);
+  d.fptr   = upload(b, fptr.data(), fptr.size());
+  d.fent   = upload(b, fent.data(), fent.size());
+  d.e_off  = upload(b, e_off.data(), e_off.size());
+  d.jptr   = upload(b, jptr.data(), jptr.size());
+  d.jent   = upload(b, jent.data(), jent.size());
+  d.je_off = upload(b, je_off.data(), je_off.size());
+  d.order  = upload(b, order.data(), order.size());
+  bool ok  = d.n && d.y_off && d.r_off && d.rtype && d.ra && d.rb && d.rc && d.rk && d.fptr &&
+            d.fent && d.e_off && d.jptr && d.jent && d.je_off && d.order;
+  ok = ok && gb300::check_cuda(cudaMalloc(&b->d_y0, sizeof(double) * b->Y), "cudaMalloc(y0)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_yout, sizeof(double) * b->Y), "cudaMalloc(yout)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_stats, sizeof(SUNBatchBDFStats) * nsys),
+                         "cudaMalloc(stats)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_next, sizeof(unsigned int)), "cudaMalloc(next)") &&
+       gb300::check_cuda(cudaEventCreate(&b->ev0), "cudaEventCreate") &&
+       gb300::check_cuda(cudaEventCreate(&b->ev1), "cudaEventCreate");
+  // Scratch for the largest grid any mode launches, so that SolveAsync
+  // allocates nothing.
+  ok = ok && ensure_scratch(b, WARPS * std::max(grid_for(b, SUNBATCHBDF_FP64),
+                                                std::max(grid_for(b, SUNBATCHBDF_MIXED),
+                                                         grid_for(b, SUNBATCHBDF_FP64_EXACT))));
+  if (!ok)
+  {
+    SUNBatchBDF_GB300_Free(b);
+    return nullptr;
+  }
+  return b;
+}
+
+int SUNBatchBDF_GB300_SetTolerances(SUNBatchBDF_GB300 b, double rtol, double atol)
+{
+  if (!b || rtol < 0 || atol < 0) return SUN_ERR_ARG_OUTOFRANGE;
+  b->rtol = rtol;
+  b->atol = atol;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SetMaxNumSteps(SUNBatchBDF_GB300 b, long mxstep)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  b->mxstep = mxstep;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SetMode(SUNBatchBDF_GB300 b, int mode)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  if (mode != SUNBATCHBDF_FP64 && mode != SUNBATCHBDF_FP64_EXACT && mode != SUNBATCHBDF_MIXED)
+    return SUN_ERR_ARG_OUTOFRANGE;
+  b->mode = mode;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SetRefinementSweeps(SUNBatchBDF_GB300 b, int sweeps)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  if (sweeps < 0 || sweeps > 8) return SUN_ERR_ARG_OUTOFRANGE;
+  b->refine = sweeps;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
+                                 double* d_yout, SUNBatchBDFStats* d_stats)
+{
+  if (!b || !d_y0 || !d_yout) return SUN_ERR_ARG_CORRUPT;
+  const int grid = grid_for(b, b->mode);
+  if (grid * WARPS > b->slots) return SUN_ERR_MEM_FAIL;
+  Params P;
+  P.p       = b->dp;
+  P.t0      = t0;
+  P.tout    = tout;
+  P.rtol    = b->rtol;
+  P.atol    = b->atol;
+  P.mxstep  = b->mxstep;
+  P.refine  = b->refine;
+  P.y0      = d_y0;
+  P.yout    = d_yout;
+  P.stats   = d_stats;
+  P.next    = b->d_next;
+  P.scratch = b->d_scratch;
+  P.pivots  = b->d_piv;
+  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned int), b->stream),
+                         "cudaMemsetAsync(queue)"))
+    return SUN_ERR_EXT_FAIL;
+  cudaEventRecord(b->ev0, b->stream);
+  cudaError_t e = (b->mode == SUNBATCHBDF_FP64_EXACT) ? launch_exact(P, grid, b->stream)
+                                                      : launch_fast(P, b->mode, grid, b->stream);
+  gb300::count_launch();
+  cudaEventRecord(b->ev1, b->stream);
+  return gb300::check_cuda(e, "k_batch_bdf launch") ? SUN_SUCCESS : SUN_ERR_EXT_FAIL;
+}
+
+int SUNBatchBDF_GB300_Solve(SUNBatchBDF_GB300 b, double t0, const double* y0, double tout,
+                            double* yout, SUNBatchBDFStats* stats)
+{
+  if (!b || !y0 || !yout) return SUN_ERR_ARG_CORRUPT;
+  const size_t ybytes = sizeof(double) * b->Y;
+  const double* dy0   = y0;
+  if (!is_device_ptr(y0))
+  {
+    if (!gb300::check_cuda(cudaMemcpyAsync(b->d_y0, y0, ybytes, cudaMemcpyHostToDevice, b->stream),
+                           "cudaMemcpyAsync(y0)"))
+      return SUN_ERR_EXT_FAIL;
+    dy0 = b->d_y0;
+  }
+  const bool dev_out       = is_device_ptr(yout);
+  double* dyo              = dev_out ? yout : b->d_yout;
+  const bool dev_stats     = stats && is_device_ptr(stats);
+  SUNBatchBDFStats* dstats = stats ? (dev_stats ? stats : b->d_stats) : nullptr;
+  int rc = SUNBatchBDF_GB300_SolveAsync(b, t0, dy0, tout, dyo, dstats);
+  if (rc != SUN_SUCCESS) return rc;
+  if (!dev_out &&
+      !gb300::check_cuda(cudaMemcpyAsync(yout, dyo, ybytes, cudaMemcpyDeviceToHost, b->stream),
+                         "cudaMemcpyAsync(yout)"))
+    return SUN_ERR_EXT_FAIL;
+  if (stats && !dev_stats &&
+      !gb300::check_cuda(cudaMemcpyAsync(stats, dstats, sizeof(SUNBatchBDFStats) * b->nsys,
+                                         cudaMemcpyDeviceToHost, b->stream),
+                         "cudaMemcpyAsync(stats)"))
+    return SUN_ERR_EXT_FAIL;
+  if (!gb300::check_cuda(cudaStreamSynchronize(b->stream), "k_batch_bdf"))
+    return SUN_ERR_EXT_FAIL;
+  cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1);
+  return SUN_SUCCESS;
+}
+
+double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b) { return b ? b->last_ms : 0.0; }
+
+void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b)
+{
+  if (!b) return;
+  cudaStreamSynchronize(b->stream);
+  for (void* p : b->allocs) cudaFree(p);
+  cudaFree(b->d_y0);
+  cudaFree(b->d_yout);
+  cudaFree(b->d_stats);
+  cudaFree(b->d_next);
+  cudaFree(b->d_scratch);
+  cudaFree(b->d_piv);
+  cudaEventDestroy(b->ev0);
+  cudaEventDestroy(b->ev1);
+  delete b;
+}
+
+}  // extern "C"

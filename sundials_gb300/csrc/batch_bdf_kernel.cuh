@@ -1,0 +1,1136 @@
+// batch_bdf_kernel.cuh -- the per-system BDF integrator, one warp per system.
+//
+// A restatement, on the device, of one CVode(tout, CV_NORMAL) call with BDF,
+// Newton, SUNLINSOL_DENSE and an analytic Jacobian (the same control flow,
+// constants and floating-point expressions as src/cvode/cvode.c:1037-3727,
+// cvode_nls.c:256-398, cvode_ls.c:1311-1800, sunnonlinsol_newton.c:179-330 and
+// sundials_dense.c:85-193).  Function names follow the reference's so the two
+// can be read side by side.
+//
+// Work layout: the 32 lanes of a warp own the elements i = lane, lane + 32 of
+// every vector of their system (n <= 64); vectors live in the warp's slice of
+// shared memory, so element-wise operations need no synchronisation; the
+// right-hand side gathers through shared memory; reductions are a fixed-order
+// butterfly (FP64, MIXED) or CVODE's sequential sum (FP64_EXACT); the dense
+// factorisation distributes the trailing-submatrix update over all lanes.
+// Every scalar of the step control is computed redundantly, and identically,
+// by all lanes, so control flow is warp-uniform.
+//
+// This header is compiled twice: batch_bdf_fast.cu (FP64 with FMA, MIXED) and
+// batch_bdf_exact.cu (FP64_EXACT, built with -fmad=false so no product and
+// sum is contracted, as in the reference built for x86-64).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/sunbatchbdf_gb300.h"
+#include "ddpow.h"
+
+namespace bdf {
+
+constexpr int NMAX  = 64;
+constexpr int QMAX  = 5;
+constexpr int RMAX  = 2 * NMAX;  // reactions per system
+constexpr int WARPS = 4;         // warps per block
+
+// CVODE defaults: cvode_impl.h:55-127, cvode.c:118-125, cvode_nls.c:32-34,
+// cvode_ls_impl.h:43-45.
+constexpr int MXNCF = 10, MXNEF = 7, MXNEF1 = 3, LONG_WAIT = 10, SMALL_NST = 10, SMALL_NEF = 2;
+constexpr int MAX_ITERS = 4, NLS_MAXCOR = 3, MSBP = 20, MSBJ = 51;
+constexpr double ETA_MAX_FX = 1.5, ETA_MAX_FS = 10000.0, ETA_MAX_ES = 10.0, ETA_MAX_GS = 10.0;
+constexpr double ETA_MIN = 0.1, ETA_MAX_EF = 0.2, ETA_MIN_EF = 0.1, ETA_CF = 0.25;
+constexpr double ADDON = 0.000001, BIAS1 = 6.0, BIAS2 = 6.0, BIAS3 = 10.0;
+constexpr double HLB_FACTOR = 100.0, HUB_FACTOR = 0.1, CORTES = 0.1;
+constexpr double CRDOWN = 0.3, RDIV = 2.0, DGMAX_LSETUP = 0.3, DGMAX_JBAD = 0.2;
+constexpr double UROUND = 0x1p-52;  // DBL_EPSILON, SUN_UNIT_ROUNDOFF
+
+enum { FIRST_CALL = 6, PREV_CONV_FAIL = 7, PREV_ERR_FAIL = 9 };
+enum { NO_FAILURES = 0, FAIL_BAD_J = 1, FAIL_OTHER = 2 };
+enum { R_SUCCESS = 0, R_CONTINUE = 901, R_CONV_RECVR = 902 };
+enum { DO_ERROR_TEST = 2, PREDICT_AGAIN = 3, TRY_AGAIN = 5 };
+enum { CV_SUCCESS = 0, CV_TOO_MUCH_WORK = -1, CV_TOO_MUCH_ACC = -2, CV_ERR_FAILURE = -3,
+       CV_CONV_FAILURE = -4 };
+
+// Device-side problem: the host arrays plus the two CSR indexes built at
+// creation (species -> signed reactions for f, reactant -> reactions for J).
+struct DevProblem
+{
+  int64_t nsys;
+  const int32_t* n;
+  const int64_t* y_off;
+  const int64_t* r_off;
+  const int32_t* rtype;
+  const int32_t* ra;
+  const int32_t* rb;
+  const int32_t* rc;
+  const double* rk;
+  const int32_t* fptr;   // [y_off[s] + s + i], local offsets into fent
+  const int32_t* fent;   // [e_off[s] + e] = r << 1 | (1 if the rate is subtracted)
+  const int64_t* e_off;  // [nsys+1]
+  const int32_t* jptr;   // [y_off[s] + s + j], local offsets into jent
+  const int32_t* jent;   // [je_off[s] + e] = r << 1 | (1 if j is reactant B)
+  const int64_t* je_off; // [nsys+1]
+  const int32_t* order;  // processing order (largest systems first)
+};
+
+struct Params
+{
+  DevProblem p;
+  double t0, tout, rtol, atol;
+  long mxstep;
+  int refine;
+  const double* y0;
+  double* yout;
+  SUNBatchBDFStats* stats;
+  unsigned int* next;      // work-queue head
+  double* scratch;         // per warp slot: savedJ (NMAX^2), M (NMAX^2) doubles
+  int* pivots;             // per warp slot: NMAX
+};
+
+// Per-warp shared-memory slice.
+struct WarpMem
+{
+  double zn[QMAX + 1][NMAX];
+  double ewt[NMAX], acor[NMAX], y[NMAX], tempv[NMAX], ftemp[NMAX], delta[NMAX];
+  double rate[RMAX];
+  double red[NMAX];
+};
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    double o = __shfl_xor_sync(0xffffffffu, v, off);
+    v        = o > v ? o : v;
+  }
+  return v;
+}
+__device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : b; }
+__device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
+__device__ __forceinline__ double rsqrt_sun(double x) { return x <= 0.0 ? 0.0 : sqrt(x); }
+
+// SUNRpowerR: the exact mode rounds pow correctly (double-double), the fast
+// modes use the device pow.
+template <bool EXACT>
+__device__ __forceinline__ double cv_pow(double x, double y)
+{
+  return EXACT ? dd_pow(x, y) : pow(x, y);
+}
+
+template <int MODE>
+struct Integrator
+{
+  static constexpr bool EXACT = (MODE == SUNBATCHBDF_FP64_EXACT);
+  static constexpr bool MIXED = (MODE == SUNBATCHBDF_MIXED);
+
+  const Params& P;
+  WarpMem& w;
+  const int lane;
+  // system
+  int n, nr;
+  const int32_t *rt, *ra, *rb, *rc, *fptr, *fent, *jptr, *jent;
+  const double* rk;
+  double* J;   // saved Jacobian, column-major n x n
+  double* M;   // Newton matrix / its LU (FP64 modes)
+  float* M32;  // Newton matrix / its LU (MIXED)
+  int* piv;
+  // CVODE state (identical in every lane)
+  double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu;
+  double saved_tq5, rl1, gamma, gammap, gamrat, crate, delp, acnrm;
+  double tq[6], l[QMAX + 2], tau[QMAX + 2];
+  int q, qprime, qwait, L, indx_acor, nscon, convfail, qu;
+  int nls_jcur, cv_jcur;
+  long nst, nfe, nsetups, nje, nni, ncfn, netf, nnf, nstlp, nstlj;
+
+  __device__ Integrator(const Params& p_, WarpMem& w_, int lane_) : P(p_), w(w_), lane(lane_) {}
+
+  // ------------------------------------------------------------ norms
+  // N_VWrmsNorm_Serial: sqrt(sum((x*w)^2)/n); EXACT sums sequentially.
+  __device__ double wrms(const double* x)
+  {
+    double s;
+    if (EXACT)
+    {
+      for (int i = lane; i < n; i += 32)
+      {
+        double p = x[i] * w.ewt[i];
+        w.red[i] = p * p;
+      }
+      __syncwarp();
+      s = 0.0;
+      for (int i = 0; i < n; i++) s = s + w.red[i];
+      __syncwarp();
+    }
+    else
+    {
+      double acc = 0.0;
+      for (int i = lane; i < n; i += 32)
+      {
+        double p = x[i] * w.ewt[i];
+        acc      = fma(p, p, acc);
+      }
+      s = warp_sum(acc);
+    }
+    s = s / n;
+    return rsqrt_sun(s);
+  }
+
+  __device__ void set_ewt(const double* ycur, double* wt)
+  {  // cvEwtSetSS (cvode.c:4791)
+    for (int i = lane; i < n; i += 32)
+    {
+      double t   = fabs(ycur[i]);
+      t          = P.rtol * t;
+      t          = t + P.atol;
+      w.tempv[i] = t;
+      wt[i]      = 1.0 / t;
+    }
+  }
+
+  // ------------------------------------------------------------ model
+  __device__ void rhs(const double* ysm, double* f)
+  {
+    __syncwarp();
+    for (int r = lane; r < nr; r += 32)
+    {
+      double v = rk[r] * ysm[ra[r]];
+      if (rt[r]) v = v * ysm[rb[r]];
+      w.rate[r] = v;
+    }
+    __syncwarp();
+    for (int i = lane; i < n; i += 32)
+    {
+      double acc = 0.0;
+      for (int e = fptr[i]; e < fptr[i + 1]; e++)
+      {
+        int ent  = fent[e];
+        double v = w.rate[ent >> 1];
+        acc      = (ent & 1) ? acc - v : acc + v;
+      }
+      f[i] = acc;
+    }
+    __syncwarp();
+    nfe++;
+  }
+
+  // J (zeroed first) = df/dy at w.y; lane owns columns j = lane, lane + 32.
+  __device__ void jac()
+  {
+    for (int e = lane; e < n * n; e += 32) J[e] = 0.0;
+    __syncwarp();
+    for (int j = lane; j < n; j += 32)
+    {
+      double* col = J + j * n;
+      for (int e = jptr[j]; e < jptr[j + 1]; e++)
+      {
+        int ent = jent[e];
+        int r   = ent >> 1;
+        double d;
+        if (rt[r] == 0)
+        {
+          d         = rk[r];
+          col[ra[r]] = col[ra[r]] - d;
+          col[rb[r]] = col[rb[r]] + d;
+        }
+        else
+        {
+          d          = (ent & 1) ? rk[r] * w.y[ra[r]] : rk[r] * w.y[rb[r]];
+          col[ra[r]] = col[ra[r]] - d;
+          col[rb[r]] = col[rb[r]] - d;
+          col[rc[r]] = col[rc[r]] + d;
+        }
+      }
+    }
+    __syncwarp();
+  }
+
+  // ------------------------------------------------------------ dense LU
+  // SUNDlsMat_denseGETRF on a column-major matrix; returns 0 or k+1.
+  template <class T>
+  __device__ int getrf(T* a)
+  {
+    for (int k = 0; k < n; k++)
+    {
+      T* ck  = a + k * n;
+      double best = -1.0;
+      int bi      = n;
+      for (int i = k + lane; i < n; i += 32)
+      {
+        double v = fabs((double)ck[i]);
+        if (v > best)
+        {
+          best = v;
+          bi   = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+      {
+        double ov = __shfl_xor_sync(0xffffffffu, best, off);
+        int oi    = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ov > best || (ov == best && oi < bi))
+        {
+          best = ov;
+          bi   = oi;
+        }
+      }
+      const int l = bi;
+      if (lane == 0) piv[k] = l;
+      if (ck[l] == (T)0) return k + 1;
+      if (l != k)
+        for (int j = lane; j < n; j += 32)
+        {
+          T t          = a[j * n + l];
+          a[j * n + l] = a[j * n + k];
+          a[j * n + k] = t;
+        }
+      __syncwarp();
+      const T mult = (T)1 / ck[k];
+      for (int i = k + 1 + lane; i < n; i += 32) ck[i] *= mult;
+      __syncwarp();
+      const int rows = n - k - 1;
+      const int tot  = rows * rows;
+      int jj = lane / (rows > 0 ? rows : 1), ii = lane - jj * (rows > 0 ? rows : 1);
+      for (int t = lane; t < tot; t += 32)
+      {
+        const int j = k + 1 + jj, i = k + 1 + ii;
+        const T akj = a[j * n + k];
+        if (akj != (T)0) a[j * n + i] -= akj * ck[i];
+        ii += 32;
+        while (ii >= rows)
+        {
+          ii -= rows;
+          jj++;
+        }
+      }
+      __syncwarp();
+    }
+    return 0;
+  }
+
+  // SUNDlsMat_denseGETRS with b held in registers: b0 = b[lane], b1 = b[lane+32].
+  template <class T>
+  __device__ void getrs(const T* a, T& b0, T& b1)
+  {
+    for (int k = 0; k < n; k++)
+    {
+      const int pk = piv[k];
+      if (pk != k)
+      {
+        T vk  = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+        T vp  = __shfl_sync(0xffffffffu, pk < 32 ? b0 : b1, pk & 31);
+        if (lane == (k & 31)) { if (k < 32) b0 = vp; else b1 = vp; }
+        if (lane == (pk & 31)) { if (pk < 32) b0 = vk; else b1 = vk; }
+      }
+    }
+    for (int k = 0; k < n - 1; k++)
+    {
+      const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+      const T* ck = a + k * n;
+      if (lane > k && lane < n) b0 -= ck[lane] * bk;
+      if (lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
+    }
+    for (int k = n - 1; k > 0; k--)
+    {
+      const T* ck = a + k * n;
+      if (lane == (k & 31))
+      {
+        if (k < 32) b0 /= ck[k];
+        else b1 /= ck[k];
+      }
+      const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+      if (lane < k) b0 -= ck[lane] * bk;
+      if (lane + 32 < k) b1 -= ck[lane + 32] * bk;
+    }
+    if (lane == 0) b0 /= a[0];
+  }
+
+  // ------------------------------------------------------------ lsetup / lsolve
+  // cvNlsLSetup -> cvLsSetup -> cvLsLinSys -> SUNLinSolSetup_Dense
+  __device__ int nls_lsetup(int jbad)
+  {
+    if (jbad) convfail = FAIL_BAD_J;
+    double dgamma = fabs((gamma / gammap) - 1.0);
+    int ls_jbad   = (nst == 0) || (nst >= nstlj + MSBJ) ||
+                  ((convfail == FAIL_BAD_J) && (dgamma < DGMAX_JBAD)) || (convfail == FAIL_OTHER);
+    if (ls_jbad)
+    {
+      cv_jcur = 1;
+      jac();
+    }
+    else cv_jcur = 0;
+    const double c = -gamma;
+    int lu;
+    if (MIXED)
+    {
+      for (int e = lane; e < n * n; e += 32)
+      {
+        double v = J[e] * c;
+        if ((e / n) == (e % n)) v = v + 1.0;
+        M32[e] = (float)v;
+      }
+      __syncwarp();
+      lu = getrf<float>(M32);
+    }
+    else
+    {
+      for (int e = lane; e < n * n; e += 32)
+      {
+        double v = J[e] * c;
+        if ((e / n) == (e % n)) v += 1.0;
+        M[e] = v;
+      }
+      __syncwarp();
+      lu = getrf<double>(M);
+    }
+    __syncwarp();
+    if (cv_jcur)
+    {
+      nje++;
+      nstlj = nst;
+    }
+    nsetups++;
+    nls_jcur = cv_jcur;
+    gamrat   = 1.0;
+    gammap   = gamma;
+    crate    = 1.0;
+    nstlp    = nst;
+    return lu > 0 ? R_CONV_RECVR : R_SUCCESS;
+  }
+
+  // cvNlsLSolve -> cvLsSolve (direct): b <- A^{-1} b, then the gamrat scaling.
+  __device__ void nls_lsolve(double* b)
+  {
+    double b0 = lane < n ? b[lane] : 0.0;
+    double b1 = lane + 32 < n ? b[lane + 32] : 0.0;
+    if (MIXED)
+    {
+      // FP32 solve, then FP64 refinement with r = b - (x - gammap * J x)
+      float f0 = (float)b0, f1 = (float)b1;
+      getrs<float>(M32, f0, f1);
+      double x0 = f0, x1 = f1;
+      for (int sweep = 0; sweep < P.refine; sweep++)
+      {
+        double jx0 = 0.0, jx1 = 0.0;
+        for (int j = 0; j < n; j++)
+        {
+          const double xj  = __shfl_sync(0xffffffffu, j < 32 ? x0 : x1, j & 31);
+          const double* cj = J + j * n;
+          if (lane < n) jx0 = fma(cj[lane], xj, jx0);
+          if (lane + 32 < n) jx1 = fma(cj[lane + 32], xj, jx1);
+        }
+        const double r0 = b0 - fma(-gammap, jx0, x0);
+        const double r1 = b1 - fma(-gammap, jx1, x1);
+        float d0 = (float)r0, d1 = (float)r1;
+        getrs<float>(M32, d0, d1);
+        x0 += (double)d0;
+        x1 += (double)d1;
+      }
+      b0 = x0;
+      b1 = x1;
+    }
+    else
+      getrs<double>(M, b0, b1);
+    if (gamrat != 1.0)
+    {
+      const double c = 2.0 / (1.0 + gamrat);
+      b0 *= c;
+      b1 *= c;
+    }
+    if (lane < n) b[lane] = b0;
+    if (lane + 32 < n) b[lane + 32] = b1;
+  }
+
+  // cvNlsResidual (cvode_nls.c:363)
+  __device__ void nls_residual(const double* ycor, double* res)
+  {
+    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + ycor[i];
+    rhs(w.y, w.ftemp);
+    const double a = -gamma;
+    for (int i = lane; i < n; i += 32)
+    {
+      double r = (rl1 * w.zn[1][i]) + ycor[i];
+      res[i]   = r + a * w.ftemp[i];
+    }
+  }
+
+  // cvNlsConvTest (cvode_nls.c:313)
+  __device__ int nls_convtest(const double* ycor, double tol, int mcur)
+  {
+    double del = wrms(w.delta);
+    if (mcur > 0)
+    {
+      double r = del / delp;
+      crate    = (CRDOWN * crate > r) ? CRDOWN * crate : r;
+    }
+    double dcon = del * (crate < 1.0 ? crate : 1.0) / tol;
+    if (dcon <= 1.0)
+    {
+      acnrm = (mcur == 0) ? del : wrms(ycor);
+      return R_SUCCESS;
+    }
+    if ((mcur >= 1) && (del > RDIV * delp)) return R_CONV_RECVR;
+    delp = del;
+    return R_CONTINUE;
+  }
+
+  // SUNNonlinSolSolve_Newton (sunnonlinsol_newton.c:179)
+  __device__ int newton_solve(double* ycor, double tol, int callLSetup)
+  {
+    int jbad = 0, retval = R_SUCCESS;
+    long niters = 0, nconvfails = 0;
+    for (;;)
+    {
+      int curiter = 0;
+      nls_residual(ycor, w.delta);
+      if (callLSetup)
+      {
+        retval = nls_lsetup(jbad);
+        if (retval != R_SUCCESS) break;
+      }
+      for (;;)
+      {
+        niters++;
+        for (int i = lane; i < n; i += 32) w.delta[i] = -w.delta[i];
+        __syncwarp();
+        nls_lsolve(w.delta);
+        for (int i = lane; i < n; i += 32) ycor[i] = ycor[i] + w.delta[i];
+        retval = nls_convtest(ycor, tol, curiter);
+        curiter++;
+        if (retval == R_SUCCESS)
+        {
+          nls_jcur = 0;
+          nni += niters;
+          nnf += nconvfails;
+          return R_SUCCESS;
+        }
+        if (retval != R_CONTINUE) break;
+        if (curiter >= NLS_MAXCOR)
+        {
+          retval = R_CONV_RECVR;
+          break;
+        }
+        nls_residual(ycor, w.delta);
+      }
+      if (retval > 0 && !nls_jcur)
+      {
+        nconvfails++;
+        callLSetup = 1;
+        jbad       = 1;
+        for (int i = lane; i < n; i += 32) ycor[i] = 0.0;
+        continue;
+      }
+      break;
+    }
+    nconvfails++;
+    nni += niters;
+    nnf += nconvfails;
+    return retval;
+  }
+
+  // ------------------------------------------------------------ step pieces
+  __device__ void rescale()
+  {  // cvRescale (cvode.c:2718)
+    double c = eta;
+    for (int j = 1; j <= q; j++)
+    {
+      for (int i = lane; i < n; i += 32) w.zn[j][i] *= c;
+      c = eta * c;
+    }
+    h      = hscale * eta;
+    next_h = h;
+    hscale = h;
+    nscon  = 0;
+  }
+
+  __device__ void increase_bdf()
+  {  // cvIncreaseBDF (cvode.c:2632)
+    double alpha0, alpha1, prod, xi, xiold, hsum, A1;
+    for (int i = 0; i <= QMAX; i++) l[i] = 0.0;
+    l[2] = alpha1 = prod = xiold = 1.0;
+    alpha0                       = -1.0;
+    hsum                         = hscale;
+    if (q > 1)
+      for (int j = 1; j < q; j++)
+      {
+        hsum += tau[j + 1];
+        xi = hsum / hscale;
+        prod *= xi;
+        alpha0 -= 1.0 / (j + 1);
+        alpha1 += 1.0 / xi;
+        for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xiold + l[i - 1];
+        xiold = xi;
+      }
+    A1 = (-alpha0 - alpha1) / prod;
+    for (int i = lane; i < n; i += 32) w.zn[L][i] = A1 * w.zn[indx_acor][i];
+    if (q > 1)
+      for (int j = 2; j <= q; j++)
+        for (int i = lane; i < n; i += 32) w.zn[j][i] += l[j] * w.zn[L][i];
+  }
+
+  __device__ void decrease_bdf()
+  {  // cvDecreaseBDF (cvode.c:2679)
+    double hsum, xi;
+    for (int i = 0; i <= QMAX; i++) l[i] = 0.0;
+    l[2] = 1.0;
+    hsum = 0.0;
+    for (int j = 1; j <= q - 2; j++)
+    {
+      hsum += tau[j];
+      xi = hsum / hscale;
+      for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xi + l[i - 1];
+    }
+    if (q > 2)
+      for (int j = 2; j < q; j++)
+      {
+        const double c = -l[j];
+        for (int i = lane; i < n; i += 32) w.zn[j][i] += c * w.zn[q][i];
+      }
+  }
+
+  __device__ void adjust_order(int deltaq)
+  {
+    if ((q == 2) && (deltaq != 1)) return;
+    if (deltaq == 1) increase_bdf();
+    else if (deltaq == -1) decrease_bdf();
+  }
+
+  __device__ void adjust_params()
+  {
+    if (qprime != q)
+    {
+      adjust_order(qprime - q);
+      q     = qprime;
+      L     = q + 1;
+      qwait = L;
+    }
+    rescale();
+  }
+
+  __device__ void predict()
+  {  // cvPredict (cvode.c:2748)
+    tn += h;
+    for (int k = 1; k <= q; k++)
+      for (int j = q; j >= k; j--)
+        for (int i = lane; i < n; i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] + w.zn[j][i];
+  }
+
+  __device__ void restore(double saved_t)
+  {  // cvRestore (cvode.c:3315)
+    tn = saved_t;
+    for (int k = 1; k <= q; k++)
+      for (int j = q; j >= k; j--)
+        for (int i = lane; i < n; i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] - w.zn[j][i];
+  }
+
+  __device__ void set_tq_bdf(double hsum, double alpha0, double alpha0_hat, double xi_inv,
+                             double xistar_inv)
+  {  // cvSetTqBDF (cvode.c:3022)
+    double A1 = 1.0 - alpha0_hat + alpha0;
+    double A2 = 1.0 + q * A1;
+    tq[2]     = fabs(A1 / (alpha0 * A2));
+    tq[5]     = fabs(A2 * xistar_inv / (l[q] * xi_inv));
+    if (qwait == 1)
+    {
+      if (q > 1)
+      {
+        double C     = xistar_inv / l[q];
+        double A3    = alpha0 + 1.0 / q;
+        double A4    = alpha0_hat + xi_inv;
+        double Cpinv = (1.0 - A4 + A3) / A3;
+        tq[1]        = fabs(C * Cpinv);
+      }
+      else tq[1] = 1.0;
+      hsum += tau[q];
+      xi_inv        = h / hsum;
+      double A5     = alpha0 - (1.0 / (q + 1));
+      double A6     = alpha0_hat - xi_inv;
+      double Cppinv = (1.0 - A6 + A5) / A2;
+      tq[3]         = fabs(Cppinv / (xi_inv * (q + 2) * A5));
+    }
+    tq[4] = CORTES / tq[2];
+  }
+
+  __device__ void set_bdf()
+  {  // cvSetBDF (cvode.c:2962)
+    double alpha0, alpha0_hat, xi_inv, xistar_inv, hsum;
+    l[0] = l[1] = xi_inv = xistar_inv = 1.0;
+    for (int i = 2; i <= q; i++) l[i] = 0.0;
+    alpha0 = alpha0_hat = -1.0;
+    hsum                = h;
+    if (q > 1)
+    {
+      for (int j = 2; j < q; j++)
+      {
+        hsum += tau[j - 1];
+        xi_inv = h / hsum;
+        alpha0 -= 1.0 / j;
+        for (int i = j; i >= 1; i--) l[i] += l[i - 1] * xi_inv;
+      }
+      alpha0 -= 1.0 / q;
+      xistar_inv = -l[1] - alpha0;
+      hsum += tau[q - 1];
+      xi_inv     = h / hsum;
+      alpha0_hat = -l[1] - xi_inv;
+      for (int i = q; i >= 1; i--) l[i] += l[i - 1] * xistar_inv;
+    }
+    set_tq_bdf(hsum, alpha0, alpha0_hat, xi_inv, xistar_inv);
+  }
+
+  __device__ void set_coeffs()
+  {  // cvSet (cvode.c:2791)
+    set_bdf();
+    rl1   = 1.0 / l[1];
+    gamma = h * rl1;
+    if (nst == 0) gammap = gamma;
+    gamrat = (nst > 0) ? gamma / gammap : 1.0;
+  }
+
+  __device__ int nls(int nflag)
+  {  // cvNls (cvode.c:3068)
+    convfail      = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
+    int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
+                    (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX_LSETUP);
+    for (int i = lane; i < n; i += 32) w.acor[i] = 0.0;
+    int flag = newton_solve(w.acor, tq[4], callSetup);
+    if (flag != R_SUCCESS) return flag;
+    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + w.acor[i];
+    cv_jcur = 0;
+    return R_SUCCESS;
+  }
+
+  __device__ int handle_nflag(int* nflagPtr, double saved_t, int* ncfPtr)
+  {  // cvHandleNFlag (cvode.c:3257); hmin = 0
+    int nflag = *nflagPtr;
+    if (nflag == R_SUCCESS) return DO_ERROR_TEST;
+    ncfn++;
+    restore(saved_t);
+    (*ncfPtr)++;
+    etamax = 1.0;
+    if (*ncfPtr == MXNCF) return CV_CONV_FAILURE;
+    eta       = ETA_CF;
+    *nflagPtr = PREV_CONV_FAIL;
+    rescale();
+    return PREDICT_AGAIN;
+  }
+
+  __device__ int do_error_test(int* nflagPtr, double saved_t, int* nefPtr, double* dsmPtr)
+  {  // cvDoErrorTest (cvode.c:3359); hmin = 0
+    double dsm = acnrm * tq[2];
+    *dsmPtr    = dsm;
+    if (dsm <= 1.0) return CV_SUCCESS;
+    (*nefPtr)++;
+    netf++;
+    *nflagPtr = PREV_ERR_FAIL;
+    restore(saved_t);
+    if (*nefPtr == MXNEF) return CV_ERR_FAILURE;
+    etamax = 1.0;
+    if (*nefPtr <= MXNEF1)
+    {
+      eta = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, 1.0 / L) + ADDON);
+      eta = dmax(ETA_MIN_EF, dmax(eta, 0.0));
+      if (*nefPtr >= SMALL_NEF) eta = dmin(eta, ETA_MAX_EF);
+      rescale();
+      return TRY_AGAIN;
+    }
+    if (q > 1)
+    {
+      eta = ETA_MIN_EF;
+      adjust_order(-1);
+      L = q;
+      q--;
+      qwait = L;
+      rescale();
+      return TRY_AGAIN;
+    }
+    eta = ETA_MIN_EF;
+    h *= eta;
+    next_h = h;
+    hscale = h;
+    qwait  = LONG_WAIT;
+    nscon  = 0;
+    rhs(w.zn[0], w.tempv);
+    for (int i = lane; i < n; i += 32) w.zn[1][i] = h * w.tempv[i];
+    return TRY_AGAIN;
+  }
+
+  __device__ void complete_step()
+  {  // cvCompleteStep (cvode.c:3467)
+    nst++;
+    nscon++;
+    hu = h;
+    qu = q;
+    for (int i = q; i >= 2; i--) tau[i] = tau[i - 1];
+    if ((q == 1) && (nst > 1)) tau[2] = tau[1];
+    tau[1] = h;
+    for (int j = 0; j <= q; j++)
+    {
+      const double c = l[j];
+      for (int i = lane; i < n; i += 32) w.zn[j][i] += c * w.acor[i];
+    }
+    qwait--;
+    if ((qwait == 1) && (q != QMAX))
+    {
+      for (int i = lane; i < n; i += 32) w.zn[QMAX][i] = w.acor[i];
+      saved_tq5 = tq[5];
+      indx_acor = QMAX;
+    }
+  }
+
+  __device__ void set_eta()
+  {  // cvSetEta (cvode.c:3579); eta_min_fx = 0, hmin = 0, hmax_inv = 0
+    if ((eta > 0.0) && (eta < ETA_MAX_FX))
+    {
+      eta    = 1.0;
+      hprime = h;
+    }
+    else
+    {
+      if (eta >= ETA_MAX_FX)
+      {
+        eta = dmin(eta, etamax);
+        eta /= 1.0;
+      }
+      else
+      {
+        eta = dmax(eta, ETA_MIN);
+        eta = dmax(eta, 0.0);
+      }
+      hprime = h * eta;
+      if (qprime < q) nscon = 0;
+    }
+  }
+
+  __device__ double compute_etaqm1()
+  {
+    etaqm1 = 0.0;
+    if (q > 1)
+    {
+      double ddn = wrms(w.zn[q]) * tq[1];
+      etaqm1     = 1.0 / (cv_pow<EXACT>(BIAS1 * ddn, 1.0 / q) + ADDON);
+    }
+    return etaqm1;
+  }
+
+  __device__ double compute_etaqp1()
+  {
+    etaqp1 = 0.0;
+    if (q != QMAX)
+    {
+      if (saved_tq5 == 0.0) return etaqp1;
+      double base = h / tau[2], p = 1.0;
+      for (int i = 1; i <= L; i++) p *= base;  // SUNRpowerI
+      double cquot   = (tq[5] / saved_tq5) * p;
+      const double a = -cquot;
+      for (int i = lane; i < n; i += 32) w.tempv[i] = (a * w.zn[QMAX][i]) + w.acor[i];
+      double dup = wrms(w.tempv) * tq[3];
+      etaqp1     = 1.0 / (cv_pow<EXACT>(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+    }
+    return etaqp1;
+  }
+
+  __device__ void choose_eta()
+  {  // cvChooseEta (cvode.c:3670)
+    double etam = dmax(etaqm1, dmax(etaq, etaqp1));
+    if ((etam > 0.0) && (etam < ETA_MAX_FX))
+    {
+      eta    = 1.0;
+      qprime = q;
+    }
+    else if (etam == etaq)
+    {
+      eta    = etaq;
+      qprime = q;
+    }
+    else if (etam == etaqm1)
+    {
+      eta    = etaqm1;
+      qprime = q - 1;
+    }
+    else
+    {
+      eta    = etaqp1;
+      qprime = q + 1;
+      for (int i = lane; i < n; i += 32) w.zn[QMAX][i] = w.acor[i];
+    }
+  }
+
+  __device__ void prepare_next_step(double dsm)
+  {  // cvPrepareNextStep (cvode.c:3530)
+    if (etamax == 1.0)
+    {
+      qwait  = qwait > 2 ? qwait : 2;
+      qprime = q;
+      hprime = h;
+      eta    = 1.0;
+      return;
+    }
+    etaq = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, 1.0 / L) + ADDON);
+    if (qwait != 0)
+    {
+      eta    = etaq;
+      qprime = q;
+      set_eta();
+    }
+    else
+    {
+      qwait  = 2;
+      etaqm1 = compute_etaqm1();
+      etaqp1 = compute_etaqp1();
+      choose_eta();
+      set_eta();
+    }
+  }
+
+  __device__ int step()
+  {  // cvStep (cvode.c:2367)
+    double saved_t, dsm = 0.0;
+    int ncf = 0, nef = 0, nflag, kflag, eflag;
+    if ((nst > 0) && (hprime != h)) adjust_params();
+    saved_t = tn;
+    nflag   = FIRST_CALL;
+    for (;;)
+    {
+      predict();
+      set_coeffs();
+      nflag = nls(nflag);
+      kflag = handle_nflag(&nflag, saved_t, &ncf);
+      if (kflag == PREDICT_AGAIN) continue;
+      if (kflag != DO_ERROR_TEST) return kflag;
+      eflag = do_error_test(&nflag, saved_t, &nef, &dsm);
+      if (eflag == TRY_AGAIN) continue;
+      if (eflag != CV_SUCCESS) return eflag;
+      break;
+    }
+    complete_step();
+    prepare_next_step(dsm);
+    etamax = (nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
+    for (int i = lane; i < n; i += 32) w.acor[i] *= tq[2];
+    return CV_SUCCESS;
+  }
+
+  // ------------------------------------------------------------ initial step
+  __device__ double upper_bound_h0(double tdist)
+  {  // cvUpperBoundH0 (cvode.c:2278)
+    double* temp1 = w.tempv;
+    double* temp2 = w.acor;
+    double loc    = 0.0;
+    for (int i = lane; i < n; i += 32) temp2[i] = fabs(w.zn[0][i]);
+    set_ewt(w.zn[0], temp1);
+    for (int i = lane; i < n; i += 32)
+    {
+      double t1 = 1.0 / temp1[i];
+      t1        = t1 + HUB_FACTOR * temp2[i];
+      double t2 = fabs(w.zn[1][i]);
+      t1        = t2 / t1;
+      temp1[i]  = t1;
+      loc       = fabs(t1) > loc ? fabs(t1) : loc;
+    }
+    double hub_inv = warp_max(loc);
+    double hub     = HUB_FACTOR * tdist;
+    if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
+    return hub;
+  }
+
+  __device__ double ydd_norm(double hg)
+  {  // cvYddNorm (cvode.c:2323)
+    for (int i = lane; i < n; i += 32) w.y[i] = (hg * w.zn[1][i]) + w.zn[0][i];
+    rhs(w.y, w.tempv);
+    const double a = 1.0 / hg, b = -1.0 / hg;
+    const bool sdiff = (a == -b) && (a != 1.0) && (a != -1.0);
+    for (int i = lane; i < n; i += 32)
+      w.tempv[i] = sdiff ? a * (w.tempv[i] - w.zn[1][i]) : (a * w.tempv[i]) + (b * w.zn[1][i]);
+    return wrms(w.tempv);
+  }
+
+  __device__ void hin(double tout)
+  {  // cvHin (cvode.c:2161); the right-hand side never fails here
+    double tdiff = tout - tn, hnew = 0.0;
+    int sign      = (tdiff > 0.0) ? 1 : -1;
+    double tdist  = fabs(tdiff);
+    double tround = UROUND * dmax(fabs(tn), fabs(tout));
+    double hlb    = HLB_FACTOR * tround;
+    double hub    = upper_bound_h0(tdist);
+    double hg     = rsqrt_sun(hlb * hub);
+    if (hub < hlb)
+    {
+      h = sign == -1 ? -hg : hg;
+      return;
+    }
+    for (int count1 = 1; count1 <= MAX_ITERS; count1++)
+    {
+      double yddnrm = ydd_norm(hg * sign);
+      hnew          = (yddnrm * hub * hub > 2.0) ? rsqrt_sun(2.0 / yddnrm) : rsqrt_sun(hg * hub);
+      if (count1 == MAX_ITERS) break;
+      double hrat = hnew / hg;
+      if ((hrat > 0.5) && (hrat < 2.0)) break;
+      if ((count1 > 1) && (hrat > 2.0))
+      {
+        hnew = hg;
+        break;
+      }
+      hg = hnew;
+    }
+    double h0 = 0.5 * hnew;
+    if (h0 < hlb) h0 = hlb;
+    if (h0 > hub) h0 = hub;
+    if (sign == -1) h0 = -h0;
+    h = h0;
+  }
+
+  // CVodeGetDky(t, 0) (cvode.c:1671)
+  __device__ void get_dky(double t, double* out)
+  {
+    double s = (t - tn) / h;
+    double c[QMAX + 1];
+    int js[QMAX + 1];
+    int nvec = 0;
+    for (int j = q; j >= 0; j--)
+    {
+      c[nvec] = 1.0;
+      for (int i = 0; i < j; i++) c[nvec] *= s;
+      js[nvec] = j;
+      nvec++;
+    }
+    for (int i = lane; i < n; i += 32)
+    {
+      double v;
+      if (nvec == 2) v = (c[0] * w.zn[js[0]][i]) + (c[1] * w.zn[js[1]][i]);
+      else
+      {
+        v = c[0] * w.zn[js[0]][i];
+        for (int k = 1; k < nvec; k++) v += c[k] * w.zn[js[k]][i];
+      }
+      out[i] = v;
+    }
+  }
+
+  // ------------------------------------------------------------ one system
+  __device__ void run(int64_t s, double* scratch, int* pivbuf)
+  {
+    const DevProblem& p = P.p;
+    n    = p.n[s];
+    nr   = (int)(p.r_off[s + 1] - p.r_off[s]);
+    rt   = p.rtype + p.r_off[s];
+    ra   = p.ra + p.r_off[s];
+    rb   = p.rb + p.r_off[s];
+    rc   = p.rc + p.r_off[s];
+    rk   = p.rk + p.r_off[s];
+    fptr = p.fptr + p.y_off[s] + s;
+    fent = p.fent + p.e_off[s];
+    jptr = p.jptr + p.y_off[s] + s;
+    jent = p.jent + p.je_off[s];
+    J    = scratch;
+    M    = scratch + NMAX * NMAX;
+    M32  = (float*)(scratch + NMAX * NMAX);
+    piv  = pivbuf;
+
+    const double* y0 = P.y0 + p.y_off[s];
+    for (int i = lane; i < n; i += 32) w.zn[0][i] = y0[i];
+    tn = P.t0;
+    h = hscale = hprime = next_h = eta = etaq = etaqm1 = etaqp1 = hu = 0.0;
+    saved_tq5 = rl1 = gamma = gammap = gamrat = crate = delp = acnrm = 0.0;
+    for (int i = 0; i < 6; i++) tq[i] = 0.0;
+    for (int i = 0; i < QMAX + 2; i++) l[i] = tau[i] = 0.0;
+    q = 1;
+    L = 2;
+    qwait = L;
+    qprime = 0;
+    indx_acor = 0;
+    nscon = convfail = qu = 0;
+    nls_jcur = cv_jcur = 0;
+    etamax = ETA_MAX_FS;
+    nst = nfe = nsetups = nje = nni = ncfn = netf = nnf = nstlp = nstlj = 0;
+    int istate = CV_SUCCESS;
+    const double tout = P.tout;
+
+    set_ewt(w.zn[0], w.ewt);
+    rhs(w.zn[0], w.zn[1]);
+    hin(tout);
+    hscale = h;
+    hprime = h;
+    for (int i = lane; i < n; i += 32) w.zn[1][i] *= h;
+
+    long nstloc = 0;
+    for (;;)
+    {
+      next_h = h;
+      if (nst > 0) set_ewt(w.zn[0], w.ewt);
+      if ((P.mxstep > 0) && (nstloc >= P.mxstep))
+      {
+        istate = CV_TOO_MUCH_WORK;
+        break;
+      }
+      double nrm = wrms(w.zn[0]);
+      if (UROUND * nrm > 1.0)
+      {
+        istate = CV_TOO_MUCH_ACC;
+        break;
+      }
+      int kflag = step();
+      if (kflag != CV_SUCCESS)
+      {
+        istate = kflag;
+        break;
+      }
+      nstloc++;
+      if ((tn - tout) * h >= 0.0) break;
+    }
+    double* yo = P.yout + p.y_off[s];
+    if (istate == CV_SUCCESS) get_dky(tout, yo);
+    else
+      for (int i = lane; i < n; i += 32) yo[i] = w.zn[0][i];
+    if (lane == 0 && P.stats)
+    {
+      SUNBatchBDFStats st;
+      st.nst     = nst;
+      st.nfe     = nfe;
+      st.nsetups = nsetups;
+      st.nje     = nje;
+      st.nni     = nni;
+      st.ncfn    = ncfn;
+      st.netf    = netf;
+      st.nnf     = nnf;
+      st.flag    = istate;
+      st.qu      = qu;
+      st.tn      = tn;
+      st.hu      = hu;
+      P.stats[s] = st;
+    }
+    __syncwarp();
+  }
+};
+
+// Persistent kernel: each warp takes the next system from the queue until
+// the queue is empty (no waiting on other warps or blocks).
+template <int MODE>
+__global__ void __launch_bounds__(WARPS * 32) k_batch_bdf(Params P)
+{
+  __shared__ WarpMem mem[WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = blockIdx.x * WARPS + warp;
+  double* scratch = P.scratch + (size_t)slot * (2 * NMAX * NMAX);
+  int* pivbuf     = P.pivots + (size_t)slot * NMAX;
+  Integrator<MODE> I(P, mem[warp], lane);
+  for (;;)
+  {
+    unsigned int idx = 0;
+    if (lane == 0) idx = atomicAdd(P.next, 1u);
+    idx = __shfl_sync(0xffffffffu, idx, 0);
+    if ((int64_t)idx >= P.p.nsys) break;
+    const int64_t s = P.p.order[idx];
+    I.run(s, scratch, pivbuf);
+  }
+}
+
+}  // namespace bdf
