@@ -96,6 +96,7 @@ struct WarpMem
   double ewt[NMAX], acor[NMAX], y[NMAX], tempv[NMAX], ftemp[NMAX], delta[NMAX];
   double rate[RMAX];
   double red[NMAX];
+  double rdiag[NMAX];
 };
 
 // ---------------------------------------------------------------- helpers
@@ -119,6 +120,37 @@ __device__ __forceinline__ double dmax(double a, double b) { return a > b ? a : 
 __device__ __forceinline__ double dmin(double a, double b) { return a < b ? a : b; }
 __device__ __forceinline__ double rsqrt_sun(double x) { return x <= 0.0 ? 0.0 : sqrt(x); }
 
+// 1.0/j for the small integers CVODE divides by (j <= 8): the same bits as
+// the run-time division, without spending FP64 instructions on it.
+__device__ __forceinline__ double inv_int(int j)
+{
+  switch (j)
+  {
+  case 1: return 1.0;
+  case 2: return 1.0 / 2.0;
+  case 3: return 1.0 / 3.0;
+  case 4: return 1.0 / 4.0;
+  case 5: return 1.0 / 5.0;
+  case 6: return 1.0 / 6.0;
+  case 7: return 1.0 / 7.0;
+  case 8: return 1.0 / 8.0;
+  default: return 1.0 / (double)j;
+  }
+}
+
+// Order-preserving integer key of |v| (IEEE bits of a non-negative value
+// compare like integers), so pivot searches need no FP64 compares.
+__device__ __forceinline__ long long abs_key(double v)
+{
+  return __double_as_longlong(v) & 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ long long abs_key(float v)
+{
+  return (long long)(__float_as_int(v) & 0x7fffffff);
+}
+__device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
+__device__ __forceinline__ bool is_zero(float v) { return (__float_as_int(v) << 1) == 0; }
+
 // SUNRpowerR: the exact mode rounds pow correctly (double-double), the fast
 // modes use the device pow.
 template <bool EXACT>
@@ -138,6 +170,9 @@ struct Integrator
   const int lane;
   // system
   int n, nr;
+  bool two;      // n > 32: lanes own a second element
+  double inv_n;  // 1/n (fast modes)
+  double* rdiag; // reciprocal pivots of the factorisation (fast modes)
   const int32_t *rt, *ra, *rb, *rc, *fptr, *fent, *jptr, *jent;
   const double* rk;
   double* J;   // saved Jacobian, column-major n x n
@@ -181,7 +216,7 @@ struct Integrator
       }
       s = warp_sum(acc);
     }
-    s = s / n;
+    s = EXACT ? s / n : s * inv_n;
     return rsqrt_sun(s);
   }
 
@@ -261,32 +296,32 @@ struct Integrator
   {
     for (int k = 0; k < n; k++)
     {
-      T* ck  = a + k * n;
-      double best = -1.0;
-      int bi      = n;
+      T* ck        = a + k * n;
+      long long bk = -1;
+      int bi       = n;
       for (int i = k + lane; i < n; i += 32)
       {
-        double v = fabs((double)ck[i]);
-        if (v > best)
+        long long v = abs_key(ck[i]);
+        if (v > bk)
         {
-          best = v;
-          bi   = i;
+          bk = v;
+          bi = i;
         }
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1)
       {
-        double ov = __shfl_xor_sync(0xffffffffu, best, off);
-        int oi    = __shfl_xor_sync(0xffffffffu, bi, off);
-        if (ov > best || (ov == best && oi < bi))
+        long long ov = __shfl_xor_sync(0xffffffffu, bk, off);
+        int oi       = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ov > bk || (ov == bk && oi < bi))
         {
-          best = ov;
-          bi   = oi;
+          bk = ov;
+          bi = oi;
         }
       }
       const int l = bi;
       if (lane == 0) piv[k] = l;
-      if (ck[l] == (T)0) return k + 1;
+      if (bk == 0) return k + 1;
       if (l != k)
         for (int j = lane; j < n; j += 32)
         {
@@ -296,6 +331,7 @@ struct Integrator
         }
       __syncwarp();
       const T mult = (T)1 / ck[k];
+      if (!EXACT && lane == 0) rdiag[k] = (double)mult;
       for (int i = k + 1 + lane; i < n; i += 32) ck[i] *= mult;
       __syncwarp();
       const int rows = n - k - 1;
@@ -305,7 +341,12 @@ struct Integrator
       {
         const int j = k + 1 + jj, i = k + 1 + ii;
         const T akj = a[j * n + k];
-        if (akj != (T)0) a[j * n + i] -= akj * ck[i];
+        if (EXACT)
+        {  // the reference skips a zero multiplier (sundials_dense.c:137)
+          if (!is_zero(akj)) a[j * n + i] -= akj * ck[i];
+        }
+        else
+          a[j * n + i] = fma(-akj, ck[i], a[j * n + i]);
         ii += 32;
         while (ii >= rows)
         {
@@ -319,6 +360,8 @@ struct Integrator
   }
 
   // SUNDlsMat_denseGETRS with b held in registers: b0 = b[lane], b1 = b[lane+32].
+  // The fast modes multiply by the reciprocal pivots kept by getrf instead of
+  // dividing (one FP64 instruction instead of a division sequence).
   template <class T>
   __device__ void getrs(const T* a, T& b0, T& b1)
   {
@@ -327,32 +370,45 @@ struct Integrator
       const int pk = piv[k];
       if (pk != k)
       {
-        T vk  = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
-        T vp  = __shfl_sync(0xffffffffu, pk < 32 ? b0 : b1, pk & 31);
+        T vk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+        T vp = __shfl_sync(0xffffffffu, pk < 32 ? b0 : b1, pk & 31);
         if (lane == (k & 31)) { if (k < 32) b0 = vp; else b1 = vp; }
         if (lane == (pk & 31)) { if (pk < 32) b0 = vk; else b1 = vk; }
       }
     }
     for (int k = 0; k < n - 1; k++)
     {
-      const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
+      const T bk  = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
       const T* ck = a + k * n;
       if (lane > k && lane < n) b0 -= ck[lane] * bk;
-      if (lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
+      if (two && lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
     }
     for (int k = n - 1; k > 0; k--)
     {
       const T* ck = a + k * n;
       if (lane == (k & 31))
       {
-        if (k < 32) b0 /= ck[k];
-        else b1 /= ck[k];
+        if (EXACT)
+        {
+          if (k < 32) b0 /= ck[k];
+          else b1 /= ck[k];
+        }
+        else
+        {
+          const T r = (T)rdiag[k];
+          if (k < 32) b0 *= r;
+          else b1 *= r;
+        }
       }
       const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
       if (lane < k) b0 -= ck[lane] * bk;
-      if (lane + 32 < k) b1 -= ck[lane + 32] * bk;
+      if (two && lane + 32 < k) b1 -= ck[lane + 32] * bk;
     }
-    if (lane == 0) b0 /= a[0];
+    if (lane == 0)
+    {
+      if (EXACT) b0 /= a[0];
+      else b0 *= (T)rdiag[0];
+    }
   }
 
   // ------------------------------------------------------------ lsetup / lsolve
@@ -373,23 +429,17 @@ struct Integrator
     int lu;
     if (MIXED)
     {
-      for (int e = lane; e < n * n; e += 32)
-      {
-        double v = J[e] * c;
-        if ((e / n) == (e % n)) v = v + 1.0;
-        M32[e] = (float)v;
-      }
+      for (int e = lane; e < n * n; e += 32) M32[e] = (float)(J[e] * c);
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) M32[i * n + i] = (float)(J[i * n + i] * c + 1.0);
       __syncwarp();
       lu = getrf<float>(M32);
     }
     else
     {
-      for (int e = lane; e < n * n; e += 32)
-      {
-        double v = J[e] * c;
-        if ((e / n) == (e % n)) v += 1.0;
-        M[e] = v;
-      }
+      for (int e = lane; e < n * n; e += 32) M[e] = J[e] * c;
+      __syncwarp();
+      for (int i = lane; i < n; i += 32) M[i * n + i] += 1.0;
       __syncwarp();
       lu = getrf<double>(M);
     }
@@ -566,7 +616,7 @@ struct Integrator
         hsum += tau[j + 1];
         xi = hsum / hscale;
         prod *= xi;
-        alpha0 -= 1.0 / (j + 1);
+        alpha0 -= inv_int(j + 1);
         alpha1 += 1.0 / xi;
         for (int i = j + 2; i >= 2; i--) l[i] = l[i] * xiold + l[i - 1];
         xiold = xi;
@@ -645,7 +695,7 @@ struct Integrator
       if (q > 1)
       {
         double C     = xistar_inv / l[q];
-        double A3    = alpha0 + 1.0 / q;
+        double A3    = alpha0 + inv_int(q);
         double A4    = alpha0_hat + xi_inv;
         double Cpinv = (1.0 - A4 + A3) / A3;
         tq[1]        = fabs(C * Cpinv);
@@ -653,7 +703,7 @@ struct Integrator
       else tq[1] = 1.0;
       hsum += tau[q];
       xi_inv        = h / hsum;
-      double A5     = alpha0 - (1.0 / (q + 1));
+      double A5     = alpha0 - inv_int(q + 1);
       double A6     = alpha0_hat - xi_inv;
       double Cppinv = (1.0 - A6 + A5) / A2;
       tq[3]         = fabs(Cppinv / (xi_inv * (q + 2) * A5));
@@ -674,10 +724,10 @@ struct Integrator
       {
         hsum += tau[j - 1];
         xi_inv = h / hsum;
-        alpha0 -= 1.0 / j;
+        alpha0 -= inv_int(j);
         for (int i = j; i >= 1; i--) l[i] += l[i - 1] * xi_inv;
       }
-      alpha0 -= 1.0 / q;
+      alpha0 -= inv_int(q);
       xistar_inv = -l[1] - alpha0;
       hsum += tau[q - 1];
       xi_inv     = h / hsum;
@@ -737,7 +787,7 @@ struct Integrator
     etamax = 1.0;
     if (*nefPtr <= MXNEF1)
     {
-      eta = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, 1.0 / L) + ADDON);
+      eta = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, inv_int(L)) + ADDON);
       eta = dmax(ETA_MIN_EF, dmax(eta, 0.0));
       if (*nefPtr >= SMALL_NEF) eta = dmin(eta, ETA_MAX_EF);
       rescale();
@@ -817,7 +867,7 @@ struct Integrator
     if (q > 1)
     {
       double ddn = wrms(w.zn[q]) * tq[1];
-      etaqm1     = 1.0 / (cv_pow<EXACT>(BIAS1 * ddn, 1.0 / q) + ADDON);
+      etaqm1     = 1.0 / (cv_pow<EXACT>(BIAS1 * ddn, inv_int(q)) + ADDON);
     }
     return etaqm1;
   }
@@ -834,7 +884,7 @@ struct Integrator
       const double a = -cquot;
       for (int i = lane; i < n; i += 32) w.tempv[i] = (a * w.zn[QMAX][i]) + w.acor[i];
       double dup = wrms(w.tempv) * tq[3];
-      etaqp1     = 1.0 / (cv_pow<EXACT>(BIAS3 * dup, 1.0 / (L + 1)) + ADDON);
+      etaqp1     = 1.0 / (cv_pow<EXACT>(BIAS3 * dup, inv_int(L + 1)) + ADDON);
     }
     return etaqp1;
   }
@@ -875,7 +925,7 @@ struct Integrator
       eta    = 1.0;
       return;
     }
-    etaq = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, 1.0 / L) + ADDON);
+    etaq = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, inv_int(L)) + ADDON);
     if (qwait != 0)
     {
       eta    = etaq;
@@ -1030,10 +1080,13 @@ struct Integrator
     fent = p.fent + p.e_off[s];
     jptr = p.jptr + p.y_off[s] + s;
     jent = p.jent + p.je_off[s];
-    J    = scratch;
-    M    = scratch + NMAX * NMAX;
-    M32  = (float*)(scratch + NMAX * NMAX);
-    piv  = pivbuf;
+    J     = scratch;
+    M     = scratch + NMAX * NMAX;
+    M32   = (float*)(scratch + NMAX * NMAX);
+    piv   = pivbuf;
+    rdiag = w.rdiag;
+    two   = n > 32;
+    inv_n = 1.0 / n;
 
     const double* y0 = P.y0 + p.y_off[s];
     for (int i = lane; i < n; i += 32) w.zn[0][i] = y0[i];

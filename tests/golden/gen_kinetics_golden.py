@@ -45,6 +45,13 @@ def main():
         for f in K.STATS_FIELDS + ["tn", "hu"]:
             out[f"{tag}_{f}"] = st[f]
         out[f"{tag}_y"] = np.concatenate(ys)
+    # FP64 oracle solution of the rtol 1e-6 sample: the reference's CVODE at
+    # rtol 1e-10, atol 1e-16 (errors of the rtol 1e-6 runs are measured
+    # against it).
+    sub = full.subset(out["r6_ids"])
+    st, ys = run(sub, 1e-10, 1e-16, 100.0)
+    assert np.all(st["flag"] == 0)
+    out["truth_y"] = np.concatenate(ys)
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT}")
 
