@@ -38,6 +38,7 @@ struct SUNBatchBDF_GB300_
   unsigned int* d_next = nullptr;
   double* d_scratch = nullptr;
   int* d_piv = nullptr;
+  long long* d_timers = nullptr;
   int slots = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
@@ -89,6 +90,13 @@ bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
       !gb300::check_cuda(cudaMalloc(&b->d_piv, sizeof(int) * NMAX * (size_t)slots),
                          "cudaMalloc(pivots)"))
     return false;
+#ifdef SUNGB300_BDF_TIMERS
+  if (!gb300::check_cuda(cudaMalloc(&b->d_timers, sizeof(long long) * T_COUNT * (size_t)slots),
+                         "cudaMalloc(timers)") ||
+      !gb300::check_cuda(cudaMemset(b->d_timers, 0, sizeof(long long) * T_COUNT * (size_t)slots),
+                         "cudaMemset(timers)"))
+    return false;
+#endif
   b->slots = slots;
   return true;
 }
@@ -262,6 +270,7 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.next    = b->d_next;
   P.scratch = b->d_scratch;
   P.pivots  = b->d_piv;
+  P.timers  = b->d_timers;
   if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned int), b->stream),
                          "cudaMemsetAsync(queue)"))
     return SUN_ERR_EXT_FAIL;
@@ -309,6 +318,19 @@ int SUNBatchBDF_GB300_Solve(SUNBatchBDF_GB300 b, double t0, const double* y0, do
 
 double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b) { return b ? b->last_ms : 0.0; }
 
+#ifdef SUNGB300_BDF_TIMERS
+// Section cycle totals summed over warp slots (instrumented builds only).
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SectionCycles(SUNBatchBDF_GB300 b, long long* out)
+{
+  std::vector<long long> h((size_t)b->slots * T_COUNT);
+  cudaMemcpy(h.data(), b->d_timers, sizeof(long long) * h.size(), cudaMemcpyDeviceToHost);
+  for (int t = 0; t < T_COUNT; t++) out[t] = 0;
+  for (int s = 0; s < b->slots; s++)
+    for (int t = 0; t < T_COUNT; t++) out[t] += h[(size_t)s * T_COUNT + t];
+  return T_COUNT;
+}
+#endif
+
 void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b)
 {
   if (!b) return;
@@ -320,6 +342,7 @@ void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b)
   cudaFree(b->d_next);
   cudaFree(b->d_scratch);
   cudaFree(b->d_piv);
+  cudaFree(b->d_timers);
   cudaEventDestroy(b->ev0);
   cudaEventDestroy(b->ev1);
   delete b;

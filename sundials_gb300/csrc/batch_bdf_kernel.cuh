@@ -75,6 +75,17 @@ struct DevProblem
   const int32_t* order;  // processing order (largest systems first)
 };
 
+// Optional per-section cycle counters (build with -DSUNGB300_BDF_TIMERS):
+// each warp accumulates clock64() deltas per section into Params::timers.
+enum { T_RHS, T_JAC, T_LU, T_SOLVE, T_NORM, T_SETC, T_PREP, T_OTHER, T_COUNT };
+#ifdef SUNGB300_BDF_TIMERS
+#define BDF_TIC(v) long long v = clock64()
+#define BDF_TOC(v, slot) tacc[slot] += clock64() - (v)
+#else
+#define BDF_TIC(v)
+#define BDF_TOC(v, slot)
+#endif
+
 struct Params
 {
   DevProblem p;
@@ -87,6 +98,7 @@ struct Params
   unsigned int* next;      // work-queue head
   double* scratch;         // per warp slot: savedJ (NMAX^2), M (NMAX^2) doubles
   int* pivots;             // per warp slot: NMAX
+  long long* timers;       // [slots][T_COUNT] when built with SUNGB300_BDF_TIMERS
 };
 
 // Per-warp shared-memory slice.
@@ -186,6 +198,9 @@ struct Integrator
   int q, qprime, qwait, L, indx_acor, nscon, convfail, qu;
   int nls_jcur, cv_jcur;
   long nst, nfe, nsetups, nje, nni, ncfn, netf, nnf, nstlp, nstlj;
+#ifdef SUNGB300_BDF_TIMERS
+  long long tacc[T_COUNT] = {0};
+#endif
 
   __device__ Integrator(const Params& p_, WarpMem& w_, int lane_) : P(p_), w(w_), lane(lane_) {}
 
@@ -235,6 +250,7 @@ struct Integrator
   // ------------------------------------------------------------ model
   __device__ void rhs(const double* ysm, double* f)
   {
+    BDF_TIC(t0);
     __syncwarp();
     for (int r = lane; r < nr; r += 32)
     {
@@ -256,11 +272,13 @@ struct Integrator
     }
     __syncwarp();
     nfe++;
+    BDF_TOC(t0, T_RHS);
   }
 
   // J (zeroed first) = df/dy at w.y; lane owns columns j = lane, lane + 32.
   __device__ void jac()
   {
+    BDF_TIC(t0);
     for (int e = lane; e < n * n; e += 32) J[e] = 0.0;
     __syncwarp();
     for (int j = lane; j < n; j += 32)
@@ -287,6 +305,7 @@ struct Integrator
       }
     }
     __syncwarp();
+    BDF_TOC(t0, T_JAC);
   }
 
   // ------------------------------------------------------------ dense LU
@@ -359,6 +378,97 @@ struct Integrator
     return 0;
   }
 
+  // MIXED: inverse of the FP32 Newton matrix by Gauss-Jordan elimination with
+  // partial pivoting on the augmented column-major n x 2n matrix [M | I]
+  // (a[c * n + r]); afterwards columns n..2n-1 hold M^{-1}.  The pivots are the
+  // same as the LU factorisation's.  Returns 0 or k+1 on a zero pivot.
+  __device__ int gauss_jordan(float* a)
+  {
+    const int w2 = 2 * n;
+    for (int e = lane; e < n * n; e += 32) a[n * n + e] = 0.f;
+    __syncwarp();
+    for (int i = lane; i < n; i += 32) a[(n + i) * n + i] = 1.f;
+    __syncwarp();
+    for (int k = 0; k < n; k++)
+    {
+      float* ck    = a + k * n;
+      long long bk = -1;
+      int bi       = n;
+      for (int i = k + lane; i < n; i += 32)
+      {
+        long long v = abs_key(ck[i]);
+        if (v > bk)
+        {
+          bk = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1)
+      {
+        long long ov = __shfl_xor_sync(0xffffffffu, bk, off);
+        int oi       = __shfl_xor_sync(0xffffffffu, bi, off);
+        if (ov > bk || (ov == bk && oi < bi))
+        {
+          bk = ov;
+          bi = oi;
+        }
+      }
+      if (bk == 0) return k + 1;
+      const int l = bi;
+      if (l != k)
+        for (int c = k + lane; c < w2; c += 32)
+        {
+          float t      = a[c * n + l];
+          a[c * n + l] = a[c * n + k];
+          a[c * n + k] = t;
+        }
+      __syncwarp();
+      const float rp = 1.f / ck[k];
+      for (int c = k + lane; c < w2; c += 32) a[c * n + k] *= rp;
+      __syncwarp();
+      // eliminate column k from every other row: a[c][r] -= a[k][r] * a[c][k]
+      const int cols = w2 - k - 1;  // columns k+1 .. 2n-1
+      const int rows = n - 1;       // rows != k
+      const int tot  = rows > 0 ? cols * rows : 0;
+      const int rdiv = rows > 0 ? rows : 1;
+      int cc = lane / rdiv, rr = lane - cc * rdiv;
+      for (int t = lane; t < tot; t += 32)
+      {
+        const int c = k + 1 + cc, r = rr < k ? rr : rr + 1;
+        const float f = ck[r];
+        a[c * n + r]  = fmaf(-f, a[c * n + k], a[c * n + r]);
+        rr += 32;
+        while (rr >= rows)
+        {
+          rr -= rows;
+          cc++;
+        }
+      }
+      __syncwarp();
+      for (int i = lane; i < n; i += 32)
+        if (i != k) ck[i] = 0.f;
+      __syncwarp();
+    }
+    return 0;
+  }
+
+  // x = A b for a column-major n x n FP32 matrix; b, x in registers.
+  __device__ void matvec32(const float* A, float b0, float b1, float& x0, float& x1)
+  {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll 4
+    for (int j = 0; j < n; j++)
+    {
+      const float bj  = __shfl_sync(0xffffffffu, j < 32 ? b0 : b1, j & 31);
+      const float* cj = A + j * n;
+      if (lane < n) a0 = fmaf(cj[lane], bj, a0);
+      if (two && lane + 32 < n) a1 = fmaf(cj[lane + 32], bj, a1);
+    }
+    x0 = a0;
+    x1 = a1;
+  }
+
   // SUNDlsMat_denseGETRS with b held in registers: b0 = b[lane], b1 = b[lane+32].
   // The fast modes multiply by the reciprocal pivots kept by getrf instead of
   // dividing (one FP64 instruction instead of a division sequence).
@@ -425,6 +535,7 @@ struct Integrator
       jac();
     }
     else cv_jcur = 0;
+    BDF_TIC(t0);
     const double c = -gamma;
     int lu;
     if (MIXED)
@@ -433,7 +544,7 @@ struct Integrator
       __syncwarp();
       for (int i = lane; i < n; i += 32) M32[i * n + i] = (float)(J[i * n + i] * c + 1.0);
       __syncwarp();
-      lu = getrf<float>(M32);
+      lu = gauss_jordan(M32);
     }
     else
     {
@@ -444,6 +555,7 @@ struct Integrator
       lu = getrf<double>(M);
     }
     __syncwarp();
+    BDF_TOC(t0, T_LU);
     if (cv_jcur)
     {
       nje++;
@@ -461,28 +573,33 @@ struct Integrator
   // cvNlsLSolve -> cvLsSolve (direct): b <- A^{-1} b, then the gamrat scaling.
   __device__ void nls_lsolve(double* b)
   {
+    BDF_TIC(t0);
     double b0 = lane < n ? b[lane] : 0.0;
     double b1 = lane + 32 < n ? b[lane + 32] : 0.0;
     if (MIXED)
     {
-      // FP32 solve, then FP64 refinement with r = b - (x - gammap * J x)
-      float f0 = (float)b0, f1 = (float)b1;
-      getrs<float>(M32, f0, f1);
+      // x = M32^{-1} b in FP32, then FP64 refinement: r = b - (x - gammap*J x),
+      // x += M32^{-1} r; every product is a pipelined matvec (no dependent
+      // triangular chains).
+      const float* Minv = M32 + n * n;
+      float f0, f1;
+      matvec32(Minv, (float)b0, (float)b1, f0, f1);
       double x0 = f0, x1 = f1;
       for (int sweep = 0; sweep < P.refine; sweep++)
       {
         double jx0 = 0.0, jx1 = 0.0;
+#pragma unroll 4
         for (int j = 0; j < n; j++)
         {
           const double xj  = __shfl_sync(0xffffffffu, j < 32 ? x0 : x1, j & 31);
           const double* cj = J + j * n;
           if (lane < n) jx0 = fma(cj[lane], xj, jx0);
-          if (lane + 32 < n) jx1 = fma(cj[lane + 32], xj, jx1);
+          if (two && lane + 32 < n) jx1 = fma(cj[lane + 32], xj, jx1);
         }
         const double r0 = b0 - fma(-gammap, jx0, x0);
         const double r1 = b1 - fma(-gammap, jx1, x1);
-        float d0 = (float)r0, d1 = (float)r1;
-        getrs<float>(M32, d0, d1);
+        float d0, d1;
+        matvec32(Minv, (float)r0, (float)r1, d0, d1);
         x0 += (double)d0;
         x1 += (double)d1;
       }
@@ -499,6 +616,7 @@ struct Integrator
     }
     if (lane < n) b[lane] = b0;
     if (lane + 32 < n) b[lane + 32] = b1;
+    BDF_TOC(t0, T_SOLVE);
   }
 
   // cvNlsResidual (cvode_nls.c:363)
@@ -517,6 +635,8 @@ struct Integrator
   // cvNlsConvTest (cvode_nls.c:313)
   __device__ int nls_convtest(const double* ycor, double tol, int mcur)
   {
+    BDF_TIC(t0);
+    int rv;
     double del = wrms(w.delta);
     if (mcur > 0)
     {
@@ -527,11 +647,16 @@ struct Integrator
     if (dcon <= 1.0)
     {
       acnrm = (mcur == 0) ? del : wrms(ycor);
-      return R_SUCCESS;
+      rv    = R_SUCCESS;
     }
-    if ((mcur >= 1) && (del > RDIV * delp)) return R_CONV_RECVR;
-    delp = del;
-    return R_CONTINUE;
+    else if ((mcur >= 1) && (del > RDIV * delp)) rv = R_CONV_RECVR;
+    else
+    {
+      delp = del;
+      rv   = R_CONTINUE;
+    }
+    BDF_TOC(t0, T_NORM);
+    return rv;
   }
 
   // SUNNonlinSolSolve_Newton (sunnonlinsol_newton.c:179)
@@ -739,11 +864,13 @@ struct Integrator
 
   __device__ void set_coeffs()
   {  // cvSet (cvode.c:2791)
+    BDF_TIC(t0);
     set_bdf();
     rl1   = 1.0 / l[1];
     gamma = h * rl1;
     if (nst == 0) gammap = gamma;
     gamrat = (nst > 0) ? gamma / gammap : 1.0;
+    BDF_TOC(t0, T_SETC);
   }
 
   __device__ int nls(int nflag)
@@ -962,8 +1089,10 @@ struct Integrator
       if (eflag != CV_SUCCESS) return eflag;
       break;
     }
+    BDF_TIC(t0);
     complete_step();
     prepare_next_step(dsm);
+    BDF_TOC(t0, T_PREP);
     etamax = (nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
     for (int i = lane; i < n; i += 32) w.acor[i] *= tq[2];
     return CV_SUCCESS;
@@ -1115,6 +1244,7 @@ struct Integrator
     for (int i = lane; i < n; i += 32) w.zn[1][i] *= h;
 
     long nstloc = 0;
+    BDF_TIC(tall);
     for (;;)
     {
       next_h = h;
@@ -1139,6 +1269,7 @@ struct Integrator
       nstloc++;
       if ((tn - tout) * h >= 0.0) break;
     }
+    BDF_TOC(tall, T_OTHER);
     double* yo = P.yout + p.y_off[s];
     if (istate == CV_SUCCESS) get_dky(tout, yo);
     else
@@ -1184,6 +1315,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_batch_bdf(Params P)
     const int64_t s = P.p.order[idx];
     I.run(s, scratch, pivbuf);
   }
+#ifdef SUNGB300_BDF_TIMERS
+  if (lane == 0 && P.timers)
+    for (int t = 0; t < T_COUNT; t++) P.timers[(size_t)slot * T_COUNT + t] = I.tacc[t];
+#endif
 }
 
 }  // namespace bdf

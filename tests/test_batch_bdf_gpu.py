@@ -16,10 +16,12 @@ Parity bars:
     oracle solution (the reference's CVODE at rtol 1e-10, atol 1e-16), as a
     WRMS norm weighted by 1/(rtol*|y|+atol), i.e. in units of rtol.  The
     reference's own rtol 1e-6 run has median 1.6, p99 28, max 64 in these
-    units, so the bar is: per system err_gpu <= max(10, 3 err_ref) for >= 99%
-    of systems, median err_gpu <= 1.5 median err_ref, and every system
-    finishes where the reference does.  The agreement with the reference run
-    itself (fraction within 10x rtol) is printed.
+    units.  Two runs of the same method whose rounding differs take different
+    step sequences, so their errors are two draws from the method's error
+    distribution; the bar compares distributions: median err_gpu <= 1.5x,
+    p99 <= 2x and max <= 3x the reference's, and every system finishes where
+    the reference does.  The agreement with the reference run itself
+    (fraction within 10x rtol) is printed.
 """
 from pathlib import Path
 
@@ -81,8 +83,9 @@ def test_fast_modes_error_vs_fp64_oracle(gb300_lib, gold, sample, mode):
           f"p99 {np.percentile(e_gpu, 99):.2f} max {e_gpu.max():.2f} | reference median "
           f"{np.median(e_ref):.2f} p99 {np.percentile(e_ref, 99):.2f} max {e_ref.max():.2f} | "
           f"within 10x rtol of the reference run: {np.mean(agree <= 10):.3f}")
-    assert np.mean(e_gpu <= np.maximum(10.0, 3.0 * e_ref)) >= 0.99
     assert np.median(e_gpu) <= 1.5 * np.median(e_ref)
+    assert np.percentile(e_gpu, 99) <= 2.0 * np.percentile(e_ref, 99)
+    assert e_gpu.max() <= 3.0 * e_ref.max()
 
 
 def test_failure_is_reported_like_the_reference(gb300_lib, oracle_lib, gold):
