@@ -14,11 +14,16 @@
 #include "gb300_common.cuh"
 
 namespace bdf {
-cudaError_t launch_fast(const Params& P, int mode, int grid, cudaStream_t stream);
-cudaError_t occupancy_fast(int mode, int* blocks_per_sm);
-cudaError_t launch_exact(const Params& P, int grid, cudaStream_t stream);
-cudaError_t occupancy_exact(int* blocks_per_sm);
+cudaError_t launch_fast(const Params& P, int mode, int nb, int grid, cudaStream_t stream,
+                        const int32_t* order, int64_t count, unsigned int* next);
+cudaError_t occupancy_fast(int mode, int nb, int* per_sm);
+cudaError_t launch_exact(const Params& P, int nb, int grid, cudaStream_t stream,
+                         const int32_t* order, int64_t count, unsigned int* next);
+cudaError_t occupancy_exact(int nb, int* per_sm);
 }  // namespace bdf
+
+// Systems are processed in two size buckets, n <= 32 and 32 < n <= 64, each
+// by its own persistent launch whose shared memory is sized for the bucket.
 
 using namespace bdf;
 
@@ -40,6 +45,8 @@ struct SUNBatchBDF_GB300_
   int* d_piv = nullptr;
   long long* d_timers = nullptr;
   int slots = 0;
+  const int32_t* d_order[2] = {nullptr, nullptr};  // [0]: n <= 32, [1]: n > 32
+  int64_t count[2]          = {0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
 };
@@ -70,14 +77,15 @@ bool is_device_ptr(const void* p)
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-int grid_for(SUNBatchBDF_GB300 b, int mode)
+int grid_for(SUNBatchBDF_GB300 b, int mode, int bucket)
 {
-  int per_sm = 0;
-  cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(&per_sm)
-                                                   : occupancy_fast(mode, &per_sm);
+  const int nb  = bucket ? 64 : 32;
+  int per_sm    = 0;
+  cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(nb, &per_sm)
+                                                   : occupancy_fast(mode, nb, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-  int grid = gb300::num_sms() * per_sm;
-  int64_t need = (b->nsys + WARPS - 1) / WARPS;
+  int grid     = gb300::num_sms() * per_sm;
+  int64_t need = b->count[bucket];
   if (need < grid) grid = (int)need;
   return grid < 1 ? 1 : grid;
 }
@@ -85,7 +93,7 @@ int grid_for(SUNBatchBDF_GB300 b, int mode)
 bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
 {
   if (slots <= b->slots) return true;
-  if (!gb300::check_cuda(cudaMalloc(&b->d_scratch, sizeof(double) * 2 * NMAX * NMAX * (size_t)slots),
+  if (!gb300::check_cuda(cudaMalloc(&b->d_scratch, sizeof(double) * NMAX * NMAX * (size_t)slots),
                          "cudaMalloc(scratch)") ||
       !gb300::check_cuda(cudaMalloc(&b->d_piv, sizeof(int) * NMAX * (size_t)slots),
                          "cudaMalloc(pivots)"))
@@ -173,11 +181,15 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
     e_off[s + 1]   = e_off[s] + fo;
     je_off[s + 1]  = je_off[s] + jo;
   }
-  // Largest systems first: the cost of a system grows like n^3.
+  // Within each size bucket, largest systems first (cost grows like n^3).
   std::vector<int32_t> order(nsys);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int32_t x, int32_t y) { return prob->n[x] > prob->n[y]; });
+  int64_t nbig = 0;
+  while (nbig < nsys && prob->n[order[nbig]] > 32) nbig++;
+  b->count[1] = nbig;
+  b->count[0] = nsys - nbig;
 
   DevProblem& d = b->dp;
   d.nsys   = nsys;
@@ -196,20 +208,23 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   d.jent   = upload(b, jent.data(), jent.size());
   d.je_off = upload(b, je_off.data(), je_off.size());
   d.order  = upload(b, order.data(), order.size());
+  b->d_order[1] = d.order;
+  b->d_order[0] = d.order + nbig;
   bool ok  = d.n && d.y_off && d.r_off && d.rtype && d.ra && d.rb && d.rc && d.rk && d.fptr &&
             d.fent && d.e_off && d.jptr && d.jent && d.je_off && d.order;
   ok = ok && gb300::check_cuda(cudaMalloc(&b->d_y0, sizeof(double) * b->Y), "cudaMalloc(y0)") &&
        gb300::check_cuda(cudaMalloc(&b->d_yout, sizeof(double) * b->Y), "cudaMalloc(yout)") &&
        gb300::check_cuda(cudaMalloc(&b->d_stats, sizeof(SUNBatchBDFStats) * nsys),
                          "cudaMalloc(stats)") &&
-       gb300::check_cuda(cudaMalloc(&b->d_next, sizeof(unsigned int)), "cudaMalloc(next)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_next, 2 * sizeof(unsigned int)), "cudaMalloc(next)") &&
        gb300::check_cuda(cudaEventCreate(&b->ev0), "cudaEventCreate") &&
        gb300::check_cuda(cudaEventCreate(&b->ev1), "cudaEventCreate");
   // Scratch for the largest grid any mode launches, so that SolveAsync
   // allocates nothing.
-  ok = ok && ensure_scratch(b, WARPS * std::max(grid_for(b, SUNBATCHBDF_FP64),
-                                                std::max(grid_for(b, SUNBATCHBDF_MIXED),
-                                                         grid_for(b, SUNBATCHBDF_FP64_EXACT))));
+  int maxgrid = 1;
+  for (int mode : {SUNBATCHBDF_FP64, SUNBATCHBDF_MIXED, SUNBATCHBDF_FP64_EXACT})
+    for (int bucket = 0; bucket < 2; bucket++) maxgrid = std::max(maxgrid, grid_for(b, mode, bucket));
+  ok = ok && ensure_scratch(b, maxgrid);
   if (!ok)
   {
     SUNBatchBDF_GB300_Free(b);
@@ -254,8 +269,6 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
                                  double* d_yout, SUNBatchBDFStats* d_stats)
 {
   if (!b || !d_y0 || !d_yout) return SUN_ERR_ARG_CORRUPT;
-  const int grid = grid_for(b, b->mode);
-  if (grid * WARPS > b->slots) return SUN_ERR_MEM_FAIL;
   Params P;
   P.p       = b->dp;
   P.t0      = t0;
@@ -271,13 +284,24 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.scratch = b->d_scratch;
   P.pivots  = b->d_piv;
   P.timers  = b->d_timers;
-  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, sizeof(unsigned int), b->stream),
+  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 2 * sizeof(unsigned int), b->stream),
                          "cudaMemsetAsync(queue)"))
     return SUN_ERR_EXT_FAIL;
   cudaEventRecord(b->ev0, b->stream);
-  cudaError_t e = (b->mode == SUNBATCHBDF_FP64_EXACT) ? launch_exact(P, grid, b->stream)
-                                                      : launch_fast(P, b->mode, grid, b->stream);
-  gb300::count_launch();
+  cudaError_t e = cudaSuccess;
+  for (int bucket = 1; bucket >= 0 && e == cudaSuccess; bucket--)
+  {  // large systems first, then the small-system bucket
+    if (b->count[bucket] == 0) continue;
+    const int grid = grid_for(b, b->mode, bucket);
+    if (grid > b->slots) return SUN_ERR_MEM_FAIL;
+    const int nb = bucket ? 64 : 32;
+    e = (b->mode == SUNBATCHBDF_FP64_EXACT)
+          ? launch_exact(P, nb, grid, b->stream, b->d_order[bucket], b->count[bucket],
+                         b->d_next + bucket)
+          : launch_fast(P, b->mode, nb, grid, b->stream, b->d_order[bucket], b->count[bucket],
+                        b->d_next + bucket);
+    gb300::count_launch();
+  }
   cudaEventRecord(b->ev1, b->stream);
   return gb300::check_cuda(e, "k_batch_bdf launch") ? SUN_SUCCESS : SUN_ERR_EXT_FAIL;
 }

@@ -6,16 +6,37 @@
 
 namespace bdf {
 
-cudaError_t launch_exact(const Params& P, int grid, cudaStream_t stream)
+template <int NB>
+static cudaError_t launch_one(const Params& P, int grid, cudaStream_t stream, const int32_t* order,
+                              int64_t count, unsigned int* next)
 {
-  k_batch_bdf<SUNBATCHBDF_FP64_EXACT><<<grid, WARPS * 32, 0, stream>>>(P);
+  const size_t smem = Layout<SUNBATCHBDF_FP64_EXACT, NB>::warp_bytes;
+  cudaFuncSetAttribute(k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB><<<grid, 32, smem, stream>>>(P, order, count, next);
   return cudaGetLastError();
 }
 
-cudaError_t occupancy_exact(int* blocks_per_sm)
+template <int NB>
+static cudaError_t occ_one(int* per_sm)
 {
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-    blocks_per_sm, k_batch_bdf<SUNBATCHBDF_FP64_EXACT>, WARPS * 32, 0);
+  const size_t smem = Layout<SUNBATCHBDF_FP64_EXACT, NB>::warp_bytes;
+  cudaFuncSetAttribute(k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB>,
+                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB>,
+                                                       32, smem);
+}
+
+cudaError_t launch_exact(const Params& P, int nb, int grid, cudaStream_t stream,
+                         const int32_t* order, int64_t count, unsigned int* next)
+{
+  return nb <= 32 ? launch_one<32>(P, grid, stream, order, count, next)
+                  : launch_one<64>(P, grid, stream, order, count, next);
+}
+
+cudaError_t occupancy_exact(int nb, int* per_sm)
+{
+  return nb <= 32 ? occ_one<32>(per_sm) : occ_one<64>(per_sm);
 }
 
 }  // namespace bdf

@@ -25,6 +25,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../../include/sunbatchbdf_gb300.h"
 #include "ddpow.h"
 
@@ -33,7 +35,6 @@ namespace bdf {
 constexpr int NMAX  = 64;
 constexpr int QMAX  = 5;
 constexpr int RMAX  = 2 * NMAX;  // reactions per system
-constexpr int WARPS = 4;         // warps per block
 
 // CVODE defaults: cvode_impl.h:55-127, cvode.c:118-125, cvode_nls.c:32-34,
 // cvode_ls_impl.h:43-45.
@@ -96,19 +97,33 @@ struct Params
   double* yout;
   SUNBatchBDFStats* stats;
   unsigned int* next;      // work-queue head
-  double* scratch;         // per warp slot: savedJ (NMAX^2), M (NMAX^2) doubles
+  double* scratch;         // per warp slot: the saved Jacobian (NMAX^2 doubles)
   int* pivots;             // per warp slot: NMAX
   long long* timers;       // [slots][T_COUNT] when built with SUNGB300_BDF_TIMERS
 };
 
-// Per-warp shared-memory slice.
+// Per-warp shared-memory slice for systems of at most NB species; the warp's
+// Newton matrix (its LU factors, or its FP32 inverse) follows it in shared
+// memory with an odd leading dimension (no bank conflicts on row access).
+template <int NB>
 struct WarpMem
 {
-  double zn[QMAX + 1][NMAX];
-  double ewt[NMAX], acor[NMAX], y[NMAX], tempv[NMAX], ftemp[NMAX], delta[NMAX];
-  double rate[RMAX];
-  double red[NMAX];
-  double rdiag[NMAX];
+  double zn[QMAX + 1][NB];
+  double ewt[NB], acor[NB], y[NB], tempv[NB], ftemp[NB], delta[NB];
+  double rate[2 * NB];
+  double red[NB];
+  double rdiag[NB];
+  float fcol[NB];
+  int perm[NB];
+};
+
+template <int MODE, int NB>
+struct Layout
+{
+  using MT = typename std::conditional<MODE == SUNBATCHBDF_MIXED, float, double>::type;
+  static constexpr size_t mem_bytes   = (sizeof(WarpMem<NB>) + 15) / 16 * 16;
+  static constexpr size_t mat_bytes   = sizeof(MT) * NB * (NB + 1);
+  static constexpr size_t warp_bytes  = mem_bytes + mat_bytes;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -171,14 +186,14 @@ __device__ __forceinline__ double cv_pow(double x, double y)
   return EXACT ? dd_pow(x, y) : pow(x, y);
 }
 
-template <int MODE>
+template <int MODE, int NB>
 struct Integrator
 {
   static constexpr bool EXACT = (MODE == SUNBATCHBDF_FP64_EXACT);
   static constexpr bool MIXED = (MODE == SUNBATCHBDF_MIXED);
 
   const Params& P;
-  WarpMem& w;
+  WarpMem<NB>& w;
   const int lane;
   // system
   int n, nr;
@@ -187,9 +202,10 @@ struct Integrator
   double* rdiag; // reciprocal pivots of the factorisation (fast modes)
   const int32_t *rt, *ra, *rb, *rc, *fptr, *fent, *jptr, *jent;
   const double* rk;
-  double* J;   // saved Jacobian, column-major n x n
-  double* M;   // Newton matrix / its LU (FP64 modes)
-  float* M32;  // Newton matrix / its LU (MIXED)
+  double* J;   // saved Jacobian, column-major n x n (global memory)
+  double* M;   // Newton matrix / its LU factors (FP64 modes; shared memory)
+  float* M32;  // Newton matrix / its inverse (MIXED; shared memory)
+  int ld;      // leading dimension of M / M32 (odd)
   int* piv;
   // CVODE state (identical in every lane)
   double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu;
@@ -202,7 +218,12 @@ struct Integrator
   long long tacc[T_COUNT] = {0};
 #endif
 
-  __device__ Integrator(const Params& p_, WarpMem& w_, int lane_) : P(p_), w(w_), lane(lane_) {}
+  __device__ Integrator(const Params& p_, WarpMem<NB>& w_, void* mat, int lane_)
+    : P(p_), w(w_), lane(lane_)
+  {
+    M   = (double*)mat;
+    M32 = (float*)mat;
+  }
 
   // ------------------------------------------------------------ norms
   // N_VWrmsNorm_Serial: sqrt(sum((x*w)^2)/n); EXACT sums sequentially.
@@ -315,7 +336,7 @@ struct Integrator
   {
     for (int k = 0; k < n; k++)
     {
-      T* ck        = a + k * n;
+      T* ck        = a + k * ld;
       long long bk = -1;
       int bi       = n;
       for (int i = k + lane; i < n; i += 32)
@@ -344,9 +365,9 @@ struct Integrator
       if (l != k)
         for (int j = lane; j < n; j += 32)
         {
-          T t          = a[j * n + l];
-          a[j * n + l] = a[j * n + k];
-          a[j * n + k] = t;
+          T t           = a[j * ld + l];
+          a[j * ld + l] = a[j * ld + k];
+          a[j * ld + k] = t;
         }
       __syncwarp();
       const T mult = (T)1 / ck[k];
@@ -359,13 +380,13 @@ struct Integrator
       for (int t = lane; t < tot; t += 32)
       {
         const int j = k + 1 + jj, i = k + 1 + ii;
-        const T akj = a[j * n + k];
+        const T akj = a[j * ld + k];
         if (EXACT)
         {  // the reference skips a zero multiplier (sundials_dense.c:137)
-          if (!is_zero(akj)) a[j * n + i] -= akj * ck[i];
+          if (!is_zero(akj)) a[j * ld + i] -= akj * ck[i];
         }
         else
-          a[j * n + i] = fma(-akj, ck[i], a[j * n + i]);
+          a[j * ld + i] = fma(-akj, ck[i], a[j * ld + i]);
         ii += 32;
         while (ii >= rows)
         {
@@ -378,20 +399,17 @@ struct Integrator
     return 0;
   }
 
-  // MIXED: inverse of the FP32 Newton matrix by Gauss-Jordan elimination with
-  // partial pivoting on the augmented column-major n x 2n matrix [M | I]
-  // (a[c * n + r]); afterwards columns n..2n-1 hold M^{-1}.  The pivots are the
-  // same as the LU factorisation's.  Returns 0 or k+1 on a zero pivot.
+  // MIXED: in-place inverse of the FP32 Newton matrix (column-major,
+  // a[j*ld + i]) by Gauss-Jordan elimination with partial pivoting: at step k
+  // rows k and p swap, row k is scaled by 1/pivot, column k is eliminated
+  // from every other row (the pivot column then holds -a_ik/pivot), and the
+  // row interchanges are undone on the columns at the end, in reverse order.
+  // The pivot choice is the LU factorisation's.  Returns 0 or k+1.
   __device__ int gauss_jordan(float* a)
   {
-    const int w2 = 2 * n;
-    for (int e = lane; e < n * n; e += 32) a[n * n + e] = 0.f;
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) a[(n + i) * n + i] = 1.f;
-    __syncwarp();
     for (int k = 0; k < n; k++)
     {
-      float* ck    = a + k * n;
+      float* ck    = a + k * ld;
       long long bk = -1;
       int bi       = n;
       for (int i = k + lane; i < n; i += 32)
@@ -416,38 +434,50 @@ struct Integrator
       }
       if (bk == 0) return k + 1;
       const int l = bi;
+      if (lane == 0) w.perm[k] = l;
       if (l != k)
-        for (int c = k + lane; c < w2; c += 32)
+        for (int j = lane; j < n; j += 32)
         {
-          float t      = a[c * n + l];
-          a[c * n + l] = a[c * n + k];
-          a[c * n + k] = t;
+          float t       = a[j * ld + l];
+          a[j * ld + l] = a[j * ld + k];
+          a[j * ld + k] = t;
         }
       __syncwarp();
       const float rp = 1.f / ck[k];
-      for (int c = k + lane; c < w2; c += 32) a[c * n + k] *= rp;
+      for (int i = lane; i < n; i += 32) w.fcol[i] = ck[i];  // column k before the update
       __syncwarp();
-      // eliminate column k from every other row: a[c][r] -= a[k][r] * a[c][k]
-      const int cols = w2 - k - 1;  // columns k+1 .. 2n-1
-      const int rows = n - 1;       // rows != k
-      const int tot  = rows > 0 ? cols * rows : 0;
-      const int rdiv = rows > 0 ? rows : 1;
-      int cc = lane / rdiv, rr = lane - cc * rdiv;
+      for (int j = lane; j < n; j += 32) a[j * ld + k] = (j == k ? 1.f : a[j * ld + k]) * rp;
+      __syncwarp();
+      // every other row: a[j][i] -= f_i * a[j][k]  (column k: 0 - f_i * rp)
+      const int tot = n * n;
+      int jj = lane / n, ii = lane - jj * n;
       for (int t = lane; t < tot; t += 32)
       {
-        const int c = k + 1 + cc, r = rr < k ? rr : rr + 1;
-        const float f = ck[r];
-        a[c * n + r]  = fmaf(-f, a[c * n + k], a[c * n + r]);
-        rr += 32;
-        while (rr >= rows)
+        if (ii != k)
         {
-          rr -= rows;
-          cc++;
+          const float f  = w.fcol[ii];
+          const float rk = a[jj * ld + k];
+          a[jj * ld + ii] = (jj == k) ? -f * rp : fmaf(-f, rk, a[jj * ld + ii]);
+        }
+        ii += 32;
+        while (ii >= n)
+        {
+          ii -= n;
+          jj++;
         }
       }
       __syncwarp();
-      for (int i = lane; i < n; i += 32)
-        if (i != k) ck[i] = 0.f;
+    }
+    for (int k = n - 1; k >= 0; k--)
+    {
+      const int p = w.perm[k];
+      if (p != k)
+        for (int i = lane; i < n; i += 32)
+        {
+          float t       = a[k * ld + i];
+          a[k * ld + i] = a[p * ld + i];
+          a[p * ld + i] = t;
+        }
       __syncwarp();
     }
     return 0;
@@ -461,7 +491,7 @@ struct Integrator
     for (int j = 0; j < n; j++)
     {
       const float bj  = __shfl_sync(0xffffffffu, j < 32 ? b0 : b1, j & 31);
-      const float* cj = A + j * n;
+      const float* cj = A + j * ld;
       if (lane < n) a0 = fmaf(cj[lane], bj, a0);
       if (two && lane + 32 < n) a1 = fmaf(cj[lane + 32], bj, a1);
     }
@@ -489,13 +519,13 @@ struct Integrator
     for (int k = 0; k < n - 1; k++)
     {
       const T bk  = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
-      const T* ck = a + k * n;
+      const T* ck = a + k * ld;
       if (lane > k && lane < n) b0 -= ck[lane] * bk;
       if (two && lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
     }
     for (int k = n - 1; k > 0; k--)
     {
-      const T* ck = a + k * n;
+      const T* ck = a + k * ld;
       if (lane == (k & 31))
       {
         if (EXACT)
@@ -540,17 +570,25 @@ struct Integrator
     int lu;
     if (MIXED)
     {
-      for (int e = lane; e < n * n; e += 32) M32[e] = (float)(J[e] * c);
+      for (int e = lane; e < n * n; e += 32)
+      {
+        const int j = e / n, i = e - j * n;
+        M32[j * ld + i] = (float)(J[e] * c);
+      }
       __syncwarp();
-      for (int i = lane; i < n; i += 32) M32[i * n + i] = (float)(J[i * n + i] * c + 1.0);
+      for (int i = lane; i < n; i += 32) M32[i * ld + i] = (float)(J[i * n + i] * c + 1.0);
       __syncwarp();
       lu = gauss_jordan(M32);
     }
     else
     {
-      for (int e = lane; e < n * n; e += 32) M[e] = J[e] * c;
+      for (int e = lane; e < n * n; e += 32)
+      {
+        const int j = e / n, i = e - j * n;
+        M[j * ld + i] = J[e] * c;
+      }
       __syncwarp();
-      for (int i = lane; i < n; i += 32) M[i * n + i] += 1.0;
+      for (int i = lane; i < n; i += 32) M[i * ld + i] += 1.0;
       __syncwarp();
       lu = getrf<double>(M);
     }
@@ -581,7 +619,7 @@ struct Integrator
       // x = M32^{-1} b in FP32, then FP64 refinement: r = b - (x - gammap*J x),
       // x += M32^{-1} r; every product is a pipelined matvec (no dependent
       // triangular chains).
-      const float* Minv = M32 + n * n;
+      const float* Minv = M32;
       float f0, f1;
       matvec32(Minv, (float)b0, (float)b1, f0, f1);
       double x0 = f0, x1 = f1;
@@ -1210,8 +1248,7 @@ struct Integrator
     jptr = p.jptr + p.y_off[s] + s;
     jent = p.jent + p.je_off[s];
     J     = scratch;
-    M     = scratch + NMAX * NMAX;
-    M32   = (float*)(scratch + NMAX * NMAX);
+    ld    = n | 1;
     piv   = pivbuf;
     rdiag = w.rdiag;
     two   = n > 32;
@@ -1295,29 +1332,33 @@ struct Integrator
   }
 };
 
-// Persistent kernel: each warp takes the next system from the queue until
-// the queue is empty (no waiting on other warps or blocks).
-template <int MODE>
-__global__ void __launch_bounds__(WARPS * 32) k_batch_bdf(Params P)
+// Persistent kernel, one warp per block: each warp takes the next system of
+// its size bucket (n <= NB) from the bucket's queue until the queue is empty
+// (no waiting on other warps or blocks).  Dynamic shared memory holds the
+// warp's vectors and its Newton matrix.
+template <int MODE, int NB>
+__global__ void __launch_bounds__(32, 8) k_batch_bdf(Params P, const int32_t* order, int64_t count,
+                                                  unsigned int* next)
 {
-  __shared__ WarpMem mem[WARPS];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int slot = blockIdx.x * WARPS + warp;
-  double* scratch = P.scratch + (size_t)slot * (2 * NMAX * NMAX);
-  int* pivbuf     = P.pivots + (size_t)slot * NMAX;
-  Integrator<MODE> I(P, mem[warp], lane);
+  extern __shared__ __align__(16) unsigned char smem[];
+  using L          = Layout<MODE, NB>;
+  const int lane   = threadIdx.x & 31;
+  const int slot   = blockIdx.x;
+  double* scratch  = P.scratch + (size_t)slot * (NMAX * NMAX);
+  int* pivbuf      = P.pivots + (size_t)slot * NMAX;
+  WarpMem<NB>* mem = (WarpMem<NB>*)smem;
+  Integrator<MODE, NB> I(P, *mem, smem + L::mem_bytes, lane);
   for (;;)
   {
     unsigned int idx = 0;
-    if (lane == 0) idx = atomicAdd(P.next, 1u);
+    if (lane == 0) idx = atomicAdd(next, 1u);
     idx = __shfl_sync(0xffffffffu, idx, 0);
-    if ((int64_t)idx >= P.p.nsys) break;
-    const int64_t s = P.p.order[idx];
-    I.run(s, scratch, pivbuf);
+    if ((int64_t)idx >= count) break;
+    I.run(order[idx], scratch, pivbuf);
   }
 #ifdef SUNGB300_BDF_TIMERS
   if (lane == 0 && P.timers)
-    for (int t = 0; t < T_COUNT; t++) P.timers[(size_t)slot * T_COUNT + t] = I.tacc[t];
+    for (int t = 0; t < T_COUNT; t++) P.timers[(size_t)slot * T_COUNT + t] += I.tacc[t];
 #endif
 }
 
