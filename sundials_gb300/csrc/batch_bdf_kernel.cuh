@@ -374,25 +374,38 @@ struct Integrator
       if (!EXACT && lane == 0) rdiag[k] = (double)mult;
       for (int i = k + 1 + lane; i < n; i += 32) ck[i] *= mult;
       __syncwarp();
+      // trailing update, four independent elements per lane at a time
       const int rows = n - k - 1;
       const int tot  = rows * rows;
-      int jj = lane / (rows > 0 ? rows : 1), ii = lane - jj * (rows > 0 ? rows : 1);
-      for (int t = lane; t < tot; t += 32)
+      const int rdiv = rows > 0 ? rows : 1;
+      for (int t0 = lane; t0 < tot; t0 += 128)
       {
-        const int j = k + 1 + jj, i = k + 1 + ii;
-        const T akj = a[j * ld + k];
-        if (EXACT)
-        {  // the reference skips a zero multiplier (sundials_dense.c:137)
-          if (!is_zero(akj)) a[j * ld + i] -= akj * ck[i];
-        }
-        else
-          a[j * ld + i] = fma(-akj, ck[i], a[j * ld + i]);
-        ii += 32;
-        while (ii >= rows)
+        int idx[4];
+        T av[4], ak[4], ci[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
         {
-          ii -= rows;
-          jj++;
+          const int t = t0 + 32 * u;
+          const int j = t / rdiv, i = t - j * rdiv;
+          idx[u]      = t < tot ? (k + 1 + j) * ld + (k + 1 + i) : -1;
+          if (idx[u] >= 0)
+          {
+            ak[u] = a[(k + 1 + j) * ld + k];
+            ci[u] = ck[k + 1 + i];
+            av[u] = a[idx[u]];
+          }
         }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (idx[u] >= 0)
+          {
+            if (EXACT)
+            {  // the reference skips a zero multiplier (sundials_dense.c:137)
+              if (!is_zero(ak[u])) a[idx[u]] = av[u] - ak[u] * ci[u];
+            }
+            else
+              a[idx[u]] = fma(-ak[u], ci[u], av[u]);
+          }
       }
       __syncwarp();
     }
@@ -448,23 +461,30 @@ struct Integrator
       __syncwarp();
       for (int j = lane; j < n; j += 32) a[j * ld + k] = (j == k ? 1.f : a[j * ld + k]) * rp;
       __syncwarp();
-      // every other row: a[j][i] -= f_i * a[j][k]  (column k: 0 - f_i * rp)
+      // every other row: a[j][i] -= f_i * a[j][k]  (column k: 0 - f_i * rp);
+      // four independent elements per lane at a time
       const int tot = n * n;
-      int jj = lane / n, ii = lane - jj * n;
-      for (int t = lane; t < tot; t += 32)
+      for (int t0 = lane; t0 < tot; t0 += 128)
       {
-        if (ii != k)
+        int idx[4], jv[4], iv[4];
+        float av[4], rk[4], fv[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
         {
-          const float f  = w.fcol[ii];
-          const float rk = a[jj * ld + k];
-          a[jj * ld + ii] = (jj == k) ? -f * rp : fmaf(-f, rk, a[jj * ld + ii]);
+          const int t = t0 + 32 * u;
+          jv[u]       = t / n;
+          iv[u]       = t - jv[u] * n;
+          idx[u]      = (t < tot && iv[u] != k) ? jv[u] * ld + iv[u] : -1;
+          if (idx[u] >= 0)
+          {
+            fv[u] = w.fcol[iv[u]];
+            rk[u] = a[jv[u] * ld + k];
+            av[u] = a[idx[u]];
+          }
         }
-        ii += 32;
-        while (ii >= n)
-        {
-          ii -= n;
-          jj++;
-        }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (idx[u] >= 0) a[idx[u]] = (jv[u] == k) ? -fv[u] * rp : fmaf(-fv[u], rk[u], av[u]);
       }
       __syncwarp();
     }
@@ -483,20 +503,82 @@ struct Integrator
     return 0;
   }
 
-  // x = A b for a column-major n x n FP32 matrix; b, x in registers.
+  // x = A b for a column-major FP32 matrix (leading dimension ld); b, x in
+  // registers; four columns per trip, two accumulators per element.
   __device__ void matvec32(const float* A, float b0, float b1, float& x0, float& x1)
   {
-    float a0 = 0.f, a1 = 0.f;
-#pragma unroll 4
-    for (int j = 0; j < n; j++)
+    float a0 = 0.f, a1 = 0.f, c0 = 0.f, c1 = 0.f;
+    int j = 0;
+    for (; j + 4 <= n; j += 4)
     {
-      const float bj  = __shfl_sync(0xffffffffu, j < 32 ? b0 : b1, j & 31);
-      const float* cj = A + j * ld;
-      if (lane < n) a0 = fmaf(cj[lane], bj, a0);
-      if (two && lane + 32 < n) a1 = fmaf(cj[lane + 32], bj, a1);
+      float bj[4], v0[4], v1[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+      {
+        bj[u] = __shfl_sync(0xffffffffu, (j + u) < 32 ? b0 : b1, (j + u) & 31);
+        v0[u] = lane < n ? A[(j + u) * ld + lane] : 0.f;
+        v1[u] = (two && lane + 32 < n) ? A[(j + u) * ld + lane + 32] : 0.f;
+      }
+      a0 = fmaf(v0[0], bj[0], a0);
+      c0 = fmaf(v0[1], bj[1], c0);
+      a0 = fmaf(v0[2], bj[2], a0);
+      c0 = fmaf(v0[3], bj[3], c0);
+      if (two)
+      {
+        a1 = fmaf(v1[0], bj[0], a1);
+        c1 = fmaf(v1[1], bj[1], c1);
+        a1 = fmaf(v1[2], bj[2], a1);
+        c1 = fmaf(v1[3], bj[3], c1);
+      }
     }
-    x0 = a0;
-    x1 = a1;
+    for (; j < n; j++)
+    {
+      const float bj = __shfl_sync(0xffffffffu, j < 32 ? b0 : b1, j & 31);
+      if (lane < n) a0 = fmaf(A[j * ld + lane], bj, a0);
+      if (two && lane + 32 < n) a1 = fmaf(A[j * ld + lane + 32], bj, a1);
+    }
+    x0 = a0 + c0;
+    x1 = a1 + c1;
+  }
+
+  // y = J x with the saved FP64 Jacobian in global memory (column-major,
+  // leading dimension n); eight columns' loads in flight per trip.
+  __device__ void matvec_j(double x0, double x1, double& y0, double& y1)
+  {
+    double a0 = 0.0, a1 = 0.0, c0 = 0.0, c1 = 0.0;
+    int j = 0;
+    for (; j + 8 <= n; j += 8)
+    {
+      double xj[8], v0[8], v1[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++)
+      {
+        xj[u] = __shfl_sync(0xffffffffu, (j + u) < 32 ? x0 : x1, (j + u) & 31);
+        v0[u] = lane < n ? J[(j + u) * n + lane] : 0.0;
+        v1[u] = (two && lane + 32 < n) ? J[(j + u) * n + lane + 32] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; u += 2)
+      {
+        a0 = fma(v0[u], xj[u], a0);
+        c0 = fma(v0[u + 1], xj[u + 1], c0);
+      }
+      if (two)
+#pragma unroll
+        for (int u = 0; u < 8; u += 2)
+        {
+          a1 = fma(v1[u], xj[u], a1);
+          c1 = fma(v1[u + 1], xj[u + 1], c1);
+        }
+    }
+    for (; j < n; j++)
+    {
+      const double xj = __shfl_sync(0xffffffffu, j < 32 ? x0 : x1, j & 31);
+      if (lane < n) a0 = fma(J[j * n + lane], xj, a0);
+      if (two && lane + 32 < n) a1 = fma(J[j * n + lane + 32], xj, a1);
+    }
+    y0 = a0 + c0;
+    y1 = a1 + c1;
   }
 
   // SUNDlsMat_denseGETRS with b held in registers: b0 = b[lane], b1 = b[lane+32].
@@ -625,15 +707,8 @@ struct Integrator
       double x0 = f0, x1 = f1;
       for (int sweep = 0; sweep < P.refine; sweep++)
       {
-        double jx0 = 0.0, jx1 = 0.0;
-#pragma unroll 4
-        for (int j = 0; j < n; j++)
-        {
-          const double xj  = __shfl_sync(0xffffffffu, j < 32 ? x0 : x1, j & 31);
-          const double* cj = J + j * n;
-          if (lane < n) jx0 = fma(cj[lane], xj, jx0);
-          if (two && lane + 32 < n) jx1 = fma(cj[lane + 32], xj, jx1);
-        }
+        double jx0, jx1;
+        matvec_j(x0, x1, jx0, jx1);
         const double r0 = b0 - fma(-gammap, jx0, x0);
         const double r1 = b1 - fma(-gammap, jx1, x1);
         float d0, d1;
