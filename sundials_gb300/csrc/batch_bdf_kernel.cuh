@@ -97,7 +97,7 @@ struct Params
   double* yout;
   SUNBatchBDFStats* stats;
   unsigned int* next;      // work-queue head
-  double* scratch;         // per warp slot: the saved Jacobian (NMAX^2 doubles)
+  double* scratch;         // per warp slot: saved Jacobian, then the FP64 LU (2 NMAX^2)
   int* pivots;             // per warp slot: NMAX
   long long* timers;       // [slots][T_COUNT] when built with SUNGB300_BDF_TIMERS
 };
@@ -117,13 +117,19 @@ struct WarpMem
   int perm[NB];
 };
 
+// MIXED keeps its FP32 inverse in shared memory (its solves and the FP32
+// elimination are latency-bound); the FP64 modes are bound by the FP64 pipe
+// and run faster with more resident warps, so their LU factors stay in the
+// warp's global scratch (L1/L2-resident).
 template <int MODE, int NB>
 struct Layout
 {
+  static constexpr bool mat_in_smem  = (MODE == SUNBATCHBDF_MIXED);
   using MT = typename std::conditional<MODE == SUNBATCHBDF_MIXED, float, double>::type;
-  static constexpr size_t mem_bytes   = (sizeof(WarpMem<NB>) + 15) / 16 * 16;
-  static constexpr size_t mat_bytes   = sizeof(MT) * NB * (NB + 1);
-  static constexpr size_t warp_bytes  = mem_bytes + mat_bytes;
+  static constexpr size_t mem_bytes  = (sizeof(WarpMem<NB>) + 15) / 16 * 16;
+  static constexpr size_t mat_bytes  = mat_in_smem ? sizeof(MT) * NB * (NB + 1) : 0;
+  static constexpr size_t warp_bytes = mem_bytes + mat_bytes;
+  static constexpr int min_blocks    = mat_in_smem ? 8 : 12;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -1412,17 +1418,18 @@ struct Integrator
 // (no waiting on other warps or blocks).  Dynamic shared memory holds the
 // warp's vectors and its Newton matrix.
 template <int MODE, int NB>
-__global__ void __launch_bounds__(32, 8) k_batch_bdf(Params P, const int32_t* order, int64_t count,
-                                                  unsigned int* next)
+__global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
+  k_batch_bdf(Params P, const int32_t* order, int64_t count, unsigned int* next)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   using L          = Layout<MODE, NB>;
   const int lane   = threadIdx.x & 31;
   const int slot   = blockIdx.x;
-  double* scratch  = P.scratch + (size_t)slot * (NMAX * NMAX);
+  double* scratch  = P.scratch + (size_t)slot * (2 * NMAX * NMAX);
   int* pivbuf      = P.pivots + (size_t)slot * NMAX;
   WarpMem<NB>* mem = (WarpMem<NB>*)smem;
-  Integrator<MODE, NB> I(P, *mem, smem + L::mem_bytes, lane);
+  void* mat        = L::mat_in_smem ? (void*)(smem + L::mem_bytes) : (void*)(scratch + NMAX * NMAX);
+  Integrator<MODE, NB> I(P, *mem, mat, lane);
   for (;;)
   {
     unsigned int idx = 0;
