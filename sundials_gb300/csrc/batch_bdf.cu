@@ -93,7 +93,7 @@ int grid_for(SUNBatchBDF_GB300 b, int mode, int bucket)
 bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
 {
   if (slots <= b->slots) return true;
-  if (!gb300::check_cuda(cudaMalloc(&b->d_scratch, sizeof(double) * 2 * NMAX * NMAX * (size_t)slots),
+  if (!gb300::check_cuda(cudaMalloc(&b->d_scratch, sizeof(double) * SLOT_DOUBLES * (size_t)slots),
                          "cudaMalloc(scratch)") ||
       !gb300::check_cuda(cudaMalloc(&b->d_piv, sizeof(int) * NMAX * (size_t)slots),
                          "cudaMalloc(pivots)"))

@@ -35,6 +35,10 @@ namespace bdf {
 constexpr int NMAX  = 64;
 constexpr int QMAX  = 5;
 constexpr int RMAX  = 2 * NMAX;  // reactions per system
+// Global scratch of one warp slot: the saved Jacobian (n x n, leading
+// dimension n) followed by the FP64 LU factors (n x ld, ld = n | 1 <= NMAX+1).
+constexpr size_t SLOT_J       = (size_t)NMAX * NMAX;
+constexpr size_t SLOT_DOUBLES = SLOT_J + (size_t)NMAX * (NMAX + 1);
 
 // CVODE defaults: cvode_impl.h:55-127, cvode.c:118-125, cvode_nls.c:32-34,
 // cvode_ls_impl.h:43-45.
@@ -97,7 +101,7 @@ struct Params
   double* yout;
   SUNBatchBDFStats* stats;
   unsigned int* next;      // work-queue head
-  double* scratch;         // per warp slot: saved Jacobian, then the FP64 LU (2 NMAX^2)
+  double* scratch;         // per warp slot: SLOT_DOUBLES (saved Jacobian, FP64 LU)
   int* pivots;             // per warp slot: NMAX
   long long* timers;       // [slots][T_COUNT] when built with SUNGB300_BDF_TIMERS
 };
@@ -463,34 +467,41 @@ struct Integrator
         }
       __syncwarp();
       const float rp = 1.f / ck[k];
-      for (int i = lane; i < n; i += 32) w.fcol[i] = ck[i];  // column k before the update
+      // each lane owns rows i0 = lane, i1 = lane + 32; f = old a[k][i]
+      const int i0 = lane, i1 = lane + 32;
+      const float f0 = (i0 < n) ? ck[i0] : 0.f;
+      const float f1 = (two && i1 < n) ? ck[i1] : 0.f;
       __syncwarp();
       for (int j = lane; j < n; j += 32) a[j * ld + k] = (j == k ? 1.f : a[j * ld + k]) * rp;
       __syncwarp();
-      // every other row: a[j][i] -= f_i * a[j][k]  (column k: 0 - f_i * rp);
-      // four independent elements per lane at a time
-      const int tot = n * n;
-      for (int t0 = lane; t0 < tot; t0 += 128)
+      // every other row: a[j][i] -= f_i * a[j][k] (row k entry broadcast);
+      // column k becomes -f_i * rp.  Four columns per trip.
+      const bool own0 = i0 < n && i0 != k, own1 = two && i1 < n && i1 != k;
+      int j = 0;
+      for (; j + 4 <= n; j += 4)
       {
-        int idx[4], jv[4], iv[4];
-        float av[4], rk[4], fv[4];
+        float rk[4], v0[4], v1[4];
 #pragma unroll
         for (int u = 0; u < 4; u++)
         {
-          const int t = t0 + 32 * u;
-          jv[u]       = t / n;
-          iv[u]       = t - jv[u] * n;
-          idx[u]      = (t < tot && iv[u] != k) ? jv[u] * ld + iv[u] : -1;
-          if (idx[u] >= 0)
-          {
-            fv[u] = w.fcol[iv[u]];
-            rk[u] = a[jv[u] * ld + k];
-            av[u] = a[idx[u]];
-          }
+          rk[u] = a[(j + u) * ld + k];
+          v0[u] = own0 ? a[(j + u) * ld + i0] : 0.f;
+          v1[u] = own1 ? a[(j + u) * ld + i1] : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++)
-          if (idx[u] >= 0) a[idx[u]] = (jv[u] == k) ? -fv[u] * rp : fmaf(-fv[u], rk[u], av[u]);
+        {
+          const bool pc = (j + u) == k;
+          if (own0) a[(j + u) * ld + i0] = pc ? -f0 * rp : fmaf(-f0, rk[u], v0[u]);
+          if (own1) a[(j + u) * ld + i1] = pc ? -f1 * rp : fmaf(-f1, rk[u], v1[u]);
+        }
+      }
+      for (; j < n; j++)
+      {
+        const float rk = a[j * ld + k];
+        const bool pc  = j == k;
+        if (own0) a[j * ld + i0] = pc ? -f0 * rp : fmaf(-f0, rk, a[j * ld + i0]);
+        if (own1) a[j * ld + i1] = pc ? -f1 * rp : fmaf(-f1, rk, a[j * ld + i1]);
       }
       __syncwarp();
     }
@@ -1425,10 +1436,10 @@ __global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
   using L          = Layout<MODE, NB>;
   const int lane   = threadIdx.x & 31;
   const int slot   = blockIdx.x;
-  double* scratch  = P.scratch + (size_t)slot * (2 * NMAX * NMAX);
+  double* scratch  = P.scratch + (size_t)slot * SLOT_DOUBLES;
   int* pivbuf      = P.pivots + (size_t)slot * NMAX;
   WarpMem<NB>* mem = (WarpMem<NB>*)smem;
-  void* mat        = L::mat_in_smem ? (void*)(smem + L::mem_bytes) : (void*)(scratch + NMAX * NMAX);
+  void* mat        = L::mat_in_smem ? (void*)(smem + L::mem_bytes) : (void*)(scratch + SLOT_J);
   Integrator<MODE, NB> I(P, *mem, mat, lane);
   for (;;)
   {
