@@ -187,6 +187,29 @@ SUNGB300_EXPORT SUNErrCode N_VDotProdMultiLocal_GB300(int nvec, N_Vector x,
 SUNGB300_EXPORT SUNErrCode N_VDotProdMultiAllReduce_GB300(int nvec, N_Vector x,
                                                           sunrealtype* sum);
 
+/* Allocation-free dot products, for callers that cannot let the library
+ * allocate device memory (an application whose own pool owns the GPU's
+ * memory after start-up, or a service that must not call cudaMalloc, which
+ * synchronises the device, in its steady state).  This entry point has no
+ * counterpart in the reference.
+ *
+ * d_out[k] = x . Y[k] for k < nvec, with x, the nvec pointers in Y and d_out
+ * device arrays (Y itself is a host array of device pointers), length n,
+ * enqueued on cuda_stream (NULL: the legacy default stream).  Same bits as
+ * N_VDotProdMulti_GB300 on the same data.  nvec must be 1..8
+ * (SUNGB300_NOALLOC_MAXVEC): the reduction's scratch is one static device
+ * array of 8 x 1024 partial sums (64 KB plus a counter) that every GPU
+ * holds from library load to process exit; larger nvec returns
+ * SUN_ERR_ARG_OUTOFRANGE without launching.  The first call on a device
+ * looks up that array's address (make it before any stream capture).
+ * Calls share the array: calls that overlap on the GPU race.  Nothing is
+ * allocated and nothing is freed. */
+#define SUNGB300_NOALLOC_MAXVEC 8
+SUNGB300_EXPORT SUNErrCode N_VDotProdMultiNoAlloc_GB300(int nvec, const sunrealtype* x,
+                                                        const sunrealtype* const* Y,
+                                                        sunindextype n, sunrealtype* d_out,
+                                                        void* cuda_stream);
+
 SUNGB300_EXPORT SUNErrCode N_VBufSize_GB300(N_Vector x, sunindextype* size);
 SUNGB300_EXPORT SUNErrCode N_VBufPack_GB300(N_Vector x, void* buf);
 SUNGB300_EXPORT SUNErrCode N_VBufUnpack_GB300(N_Vector x, void* buf);
