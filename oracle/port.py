@@ -118,3 +118,27 @@ def bdf_batch(batch, rtol=1e-6, atol=1e-12, tout=100.0, mxstep=1000000, threads=
       mxstep, threads, yout.ctypes.data_as(_P), stats.ctypes.data)
     L.bdf_port_set_pow(0)
     return stats, yout
+
+
+def dense_lu(a_colmajor: np.ndarray):
+    """(factors, pivots, flag) of the GETRF restatement; a is (n, n) with a[j] = column j."""
+    L = lib()
+    f = L.port_dense_getrf
+    f.restype = ct.c_int
+    f.argtypes = [_P, ct.c_int64, ct.POINTER(ct.c_int64)]
+    n = a_colmajor.shape[0]
+    lu = np.ascontiguousarray(a_colmajor, dtype=np.float64).copy()
+    piv = np.zeros(n, np.int64)
+    flag = f(lu.ctypes.data_as(_P), n, piv.ctypes.data_as(ct.POINTER(ct.c_int64)))
+    return lu, piv, flag
+
+
+def dense_solve(lu: np.ndarray, piv: np.ndarray, b: np.ndarray) -> np.ndarray:
+    L = lib()
+    f = L.port_dense_getrs
+    f.restype = None
+    f.argtypes = [_P, ct.c_int64, ct.POINTER(ct.c_int64), _P]
+    x = np.ascontiguousarray(b, dtype=np.float64).copy()
+    f(np.ascontiguousarray(lu).ctypes.data_as(_P), lu.shape[0],
+      np.ascontiguousarray(piv, np.int64).ctypes.data_as(ct.POINTER(ct.c_int64)), x.ctypes.data_as(_P))
+    return x

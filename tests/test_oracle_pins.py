@@ -62,3 +62,19 @@ def test_port_matches_reference_nvector_serial(oracle_lib, gold, n):
     d = np.empty(5)
     port.call("port_dotprodmulti", 5, P(x), port.ptrs(xs), P(d), n)
     assert beq(d, g("dotprodmulti5"))
+
+
+DENSE = Path(__file__).resolve().parent / "golden" / "dense_lu.npz"
+
+
+@pytest.mark.parametrize("case", ["1", "3", "8", "17", "33", "64", "singular"])
+def test_dense_lu_port_matches_reference(oracle_lib, case):
+    """GETRF / GETRS restatement (oracle/dense_port.c) against the reference's
+    SUNDlsMat_denseGETRF / GETRS (tests/golden/dense_lu.npz): same bits."""
+    from oracle import port
+    g = dict(np.load(DENSE))
+    lu, piv, flag = port.dense_lu(g[f"a_{case}"])
+    assert flag == g[f"flag_{case}"][0]
+    assert beq(lu, g[f"lu_{case}"]) and np.array_equal(piv[:len(piv)], g[f"piv_{case}"])
+    if flag == 0:
+        assert beq(port.dense_solve(lu, piv, g[f"b_{case}"]), g[f"x_{case}"])
