@@ -101,6 +101,8 @@ SUNGB300_EXPORT SUNErrCode N_VEnableDotProdMultiLocal_GB300(N_Vector v,
  * products and sums in NVECTOR_SERIAL's order.  Inherited by clones; an
  * operation uses the mode of its output vector (of x for reductions). */
 SUNGB300_EXPORT SUNErrCode N_VSetFMA_GB300(N_Vector v, sunbooleantype use_fma);
+/* The mode set above (SUNTRUE for a vector that is not an NVECTOR_GB300). */
+SUNGB300_EXPORT sunbooleantype N_VGetFMA_GB300(N_Vector v);
 
 /* Last CUDA / argument error seen by this library on the calling thread
  * (0 = none); reading it clears it.  Errors are also reported to the

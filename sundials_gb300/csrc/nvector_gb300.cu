@@ -1717,6 +1717,12 @@ SUNErrCode N_VSetFMA_GB300(N_Vector v, sunbooleantype use_fma)
   return SUN_SUCCESS;
 }
 
+sunbooleantype N_VGetFMA_GB300(N_Vector v)
+{
+  if (!v || !v->content || !v->ops || v->ops->nvlinearsum != N_VLinearSum_GB300) return SUNTRUE;
+  return C(v)->fma ? SUNTRUE : SUNFALSE;
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------ the ops table
