@@ -261,6 +261,66 @@ def nvector_measure(args, rank, local, steps, warmup):
     return out
 
 
+def spgmr_measure(nx=2048, solves=20, warmup=3):
+    """SPGMR on the heat-2D Newton system (I - gamma J) x = b, 2048^2 interior
+    points, maxl 5, left Jacobi preconditioning, no restarts (the CVODE
+    configuration of the heat benchmark), with the operator and preconditioner
+    as C callbacks (include/heat2d_gb300.h).  Each Gram-Schmidt type runs with
+    the fused kernels and with the reference's sequence of N_Vector
+    operations on the same GPU; wall time per solve includes the host's
+    synchronisations, which is what the fusion removes."""
+    import torch
+    from sundials_gb300 import _lib
+    from sundials_gb300.heat2d import Heat2D
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.spgmr import SPGMR
+
+    lib = _lib.load()
+    n = nx * nx
+    gamma = 1e-6
+    rng = np.random.default_rng(1)
+    b = rng.uniform(-1.0, 1.0, n)
+    delta = 1e-4 * float(np.linalg.norm(b))
+    H = Heat2D(nx, nx)
+    H.set_gamma(gamma)
+    X, B = NVector(n), NVector.from_numpy(b)
+    at, pset, psol, data = H.c_callbacks()
+    out = {"workload": f"heat2d {nx}x{nx} Newton system, SPGMR maxl 5, left Jacobi",
+           "vector_length": n, "gamma": gamma, "delta": delta}
+    for gs, gname in ((1, "mgs"), (2, "cgs")):
+        for fused in (True, False):
+            S = SPGMR(X, 1, 5)
+            S.set_gs_type(gs)
+            S.set_fused(fused)
+            S.set_atimes_c(at, data)
+            S.set_preconditioner_c(psol, pset, data)
+            S.initialize()
+            S.setup()
+            for _ in range(warmup):
+                S.set_zero_guess(True)
+                S.solve(X, B, delta)
+            torch.cuda.synchronize()
+            l0 = lib.SUNGB300_KernelLaunchCount()
+            t0 = time.perf_counter()
+            for _ in range(solves):
+                S.set_zero_guess(True)
+                flag = S.solve(X, B, delta)
+            torch.cuda.synchronize()
+            el = (time.perf_counter() - t0) / solves
+            out[f"{gname}_{'fused' if fused else 'ops'}"] = {
+                "ms_per_solve": round(el * 1e3, 4), "flag": int(flag), "nli": S.num_iters,
+                "res_norm": S.res_norm, "syncs_per_solve": int(S.num_syncs),
+                "launches_per_solve": int((lib.SUNGB300_KernelLaunchCount() - l0) // solves)}
+            S.free()
+    for g in ("mgs", "cgs"):
+        out[f"{g}_fused_speedup"] = round(out[f"{g}_ops"]["ms_per_solve"]
+                                          / out[f"{g}_fused"]["ms_per_solve"], 3)
+    X.destroy()
+    B.destroy()
+    H.free()
+    return out
+
+
 def fp64_peak_tflops():
     """Dense FP64 rate of this GPU, measured live with a float64 matmul."""
     import torch
@@ -400,6 +460,7 @@ def run_kinetics(args, world, rank, local):
 
     # ---- the N_Vector microbenchmark
     nv = nvector_measure(args, rank, local, steps=10, warmup=3) if not args.no_nvector else None
+    spg = spgmr_measure() if not args.no_spgmr else None
 
     if rank != 0:
         return None
@@ -437,6 +498,8 @@ def run_kinetics(args, world, rank, local):
     }
     if nv:
         out["nvector"] = nv
+    if spg:
+        out["spgmr"] = spg
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = kinetics_cpu_sample(batch, threads=1, target_s=args.cpu_seconds)
     return out
@@ -505,7 +568,14 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nvector", action="store_true")
+    ap.add_argument("--no-spgmr", action="store_true")
+    ap.add_argument("--spgmr-only", action="store_true",
+                    help="print only the SPGMR heat-2D measurement (no kinetics line)")
+    ap.add_argument("--spgmr-solves", type=int, default=20)
     args = ap.parse_args()
+    if args.spgmr_only:
+        print(json.dumps(spgmr_measure(solves=args.spgmr_solves, warmup=args.warmup)), flush=True)
+        return
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         out = run_reference(args, world, rank)

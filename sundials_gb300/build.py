@@ -46,6 +46,7 @@ PER_FILE_FLAGS = {
     "sunlinsol_blocklu_gb300.cu": ["-fmad=false"],
     # host-side Givens QR and norm tests rounded like the reference's C
     "sunlinsol_spgmr_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "heat2d_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -107,6 +107,19 @@ class SPGMR:
         self._keep += [ps, pu]
         return self.ops["setpreconditioner"](self.S, None, pu, ps)
 
+    def set_atimes_c(self, fn_addr: int, data) -> int:
+        """ATimes given as a C function (address of a SUNATimesFn) and its data."""
+        cb = ATIMES_FN(fn_addr)
+        self._keep.append(cb)
+        return self.ops["setatimes"](self.S, data, cb)
+
+    def set_preconditioner_c(self, psolve_addr: int, psetup_addr: int | None, data) -> int:
+        """Psetup / Psolve given as C functions (SUNPSetupFn / SUNPSolveFn)."""
+        ps = PSOLVE_FN(psolve_addr)
+        pu = PSETUP_FN(psetup_addr) if psetup_addr else PSETUP_FN()
+        self._keep += [ps, pu]
+        return self.ops["setpreconditioner"](self.S, data, pu, ps)
+
     def set_scaling_vectors(self, s1=None, s2=None) -> int:
         return self.ops["setscalingvectors"](self.S, s1.v if s1 else None, s2.v if s2 else None)
 
