@@ -321,6 +321,36 @@ def spgmr_measure(nx=2048, solves=20, warmup=3):
     return out
 
 
+def learned_measure(batch, steps=2):
+    """The learned Newton predictor end to end: record training rows with the
+    plain FP64 solver on training seeds 1001-1004 (8,192 systems each), train
+    the BF16 network with the library's kernels, then solve a 16,384-system
+    slice of the test batch (every 4th system) in the MIXED form with and
+    without the predictor."""
+    from sundials_gb300 import learned
+    t0 = time.perf_counter()
+    X, T = learned.record(8192, range(learned.TRAIN_SEED0, learned.TRAIN_SEED0 + 4), 1 << 20)
+    t1 = time.perf_counter()
+    from sundials_gb300.mlp import MLP
+    net = MLP(seed=7)
+    losses = learned.train(net, X, T, epochs=8)
+    t2 = time.perf_counter()
+    sub = batch.subset(np.arange(0, batch.nsys, 4))
+    ev = learned.evaluate(sub, net, repeats=steps)
+    out = {"training_rows": int(X.shape[0]), "record_s": round(t1 - t0, 3),
+           "train_s": round(t2 - t1, 3), "loss_first_last": [losses[0], losses[-1]],
+           "target_variance": round(float(T.var().item()), 4), "systems": int(sub.nsys)}
+    for k in ("plain", "learned"):
+        r = ev[k]
+        out[k] = {"systems_per_s": round(sub.nsys / (r["kernel_ms"] / 1e3), 1),
+                  "kernel_ms": round(r["kernel_ms"], 2), "nni": r["nni"], "nfe": r["nfe"],
+                  "nst": r["nst"], "failed": r["failed"]}
+        if k == "learned":
+            out[k]["predictor_calls"], out[k]["learned_iterate_kept"] = r["calls"], r["kept"]
+    out["speedup_learned_vs_plain"] = round(ev["plain"]["kernel_ms"] / ev["learned"]["kernel_ms"], 3)
+    return out
+
+
 def fp64_peak_tflops():
     """Dense FP64 rate of this GPU, measured live with a float64 matmul."""
     import torch
@@ -461,6 +491,7 @@ def run_kinetics(args, world, rank, local):
     # ---- the N_Vector microbenchmark
     nv = nvector_measure(args, rank, local, steps=10, warmup=3) if not args.no_nvector else None
     spg = spgmr_measure() if not args.no_spgmr else None
+    lrn = learned_measure(batch) if not args.no_learned else None
 
     if rank != 0:
         return None
@@ -500,6 +531,8 @@ def run_kinetics(args, world, rank, local):
         out["nvector"] = nv
     if spg:
         out["spgmr"] = spg
+    if lrn:
+        out["learned_predictor"] = lrn
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = kinetics_cpu_sample(batch, threads=1, target_s=args.cpu_seconds)
     return out
@@ -569,6 +602,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-nvector", action="store_true")
     ap.add_argument("--no-spgmr", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--spgmr-only", action="store_true",
                     help="print only the SPGMR heat-2D measurement (no kinetics line)")
     ap.add_argument("--spgmr-solves", type=int, default=20)

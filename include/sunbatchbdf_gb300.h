@@ -109,6 +109,29 @@ SUNGB300_EXPORT int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0,
 /* Wall time of the last Solve's integration kernel in milliseconds. */
 SUNGB300_EXPORT double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b);
 
+/* Learned Newton predictor (include/sunmlp_gb300.h; no counterpart in the
+ * reference).  With device weights set, every Newton solve of the fast modes
+ * evaluates the network on its system's features and starts Newton from the
+ * network's iterate when the WRMS norm of its residual is smaller than the
+ * residual of the BDF predictor, else from the predictor (the Newton
+ * convergence test is unchanged, so is the accuracy; each solve costs one
+ * extra right-hand-side evaluation, counted in nfe).  NULL, NULL turns it
+ * off.  The exact mode ignores it. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetPredictor(SUNBatchBDF_GB300 b,
+                                                   const uint16_t* d_weights,
+                                                   const float* d_biases);
+/* Over the last solve: predictor evaluations and how often its iterate was kept. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_GetPredictorCounts(SUNBatchBDF_GB300 b, long long* calls,
+                                                         long long* kept);
+/* Training-data recorder: after every converged Newton solve of the fast
+ * modes, append the solve's features (BF16, SUNMLP_IN_PAD per row) to d_x
+ * and its converged corrector in error-weight units (64 FP32 per row, zero
+ * past n) to d_t, at row atomicAdd(d_count, 1) while it is below capacity.
+ * d_x = NULL turns it off. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetRecorder(SUNBatchBDF_GB300 b, uint16_t* d_x, float* d_t,
+                                                  long long capacity,
+                                                  unsigned long long* d_count);
+
 SUNGB300_EXPORT void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b);
 
 #ifdef __cplusplus

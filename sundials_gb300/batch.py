@@ -31,6 +31,10 @@ def _declare(lib):
         ("SUNBatchBDF_GB300_SolveAsync", ct.c_int, [vp, ct.c_double, vp, ct.c_double, vp, vp]),
         ("SUNBatchBDF_GB300_LastKernelMs", ct.c_double, [vp]),
         ("SUNBatchBDF_GB300_Free", None, [vp]),
+        ("SUNBatchBDF_GB300_SetPredictor", ct.c_int, [vp, vp, vp]),
+        ("SUNBatchBDF_GB300_GetPredictorCounts", ct.c_int,
+         [vp, ct.POINTER(ct.c_longlong), ct.POINTER(ct.c_longlong)]),
+        ("SUNBatchBDF_GB300_SetRecorder", ct.c_int, [vp, vp, vp, ct.c_longlong, vp]),
     ]:
         f = getattr(lib, name)
         f.restype = res
@@ -80,6 +84,29 @@ class BatchBDF:
         rc = self.lib.SUNBatchBDF_GB300_SolveAsync(self.h, t0, d_y0, tout, d_yout, d_stats)
         if rc != 0:
             raise RuntimeError(f"SUNBatchBDF_GB300_SolveAsync failed ({rc})")
+
+    def set_predictor(self, mlp) -> None:
+        """Use a trained sundials_gb300.mlp.MLP as Newton predictor (None: off)."""
+        if mlp is None:
+            rc = self.lib.SUNBatchBDF_GB300_SetPredictor(self.h, None, None)
+        else:
+            rc = self.lib.SUNBatchBDF_GB300_SetPredictor(self.h, mlp.device_weights,
+                                                         mlp.device_biases)
+        if rc != 0:
+            raise RuntimeError(f"SUNBatchBDF_GB300_SetPredictor failed ({rc})")
+        self._mlp = mlp
+
+    def predictor_counts(self):
+        calls, kept = ct.c_longlong(), ct.c_longlong()
+        assert self.lib.SUNBatchBDF_GB300_GetPredictorCounts(self.h, ct.byref(calls),
+                                                             ct.byref(kept)) == 0
+        return calls.value, kept.value
+
+    def set_recorder(self, d_x: int, d_t: int, capacity: int, d_count: int) -> None:
+        """Record (features, converged corrector) rows into device buffers."""
+        rc = self.lib.SUNBatchBDF_GB300_SetRecorder(self.h, d_x, d_t, capacity, d_count)
+        if rc != 0:
+            raise RuntimeError(f"SUNBatchBDF_GB300_SetRecorder failed ({rc})")
 
     @property
     def last_kernel_ms(self) -> float:

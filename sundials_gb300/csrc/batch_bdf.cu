@@ -49,6 +49,14 @@ struct SUNBatchBDF_GB300_
   int64_t count[2]          = {0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
+  // learned predictor and training-data recorder
+  const uint16_t* mlp_w = nullptr;
+  const float* mlp_b    = nullptr;
+  unsigned long long* d_lp = nullptr;  // [2] predictor calls, learned iterate kept
+  uint16_t* rec_x = nullptr;
+  float* rec_t    = nullptr;
+  unsigned long long* rec_count = nullptr;
+  long long rec_cap = 0;
 };
 
 namespace {
@@ -265,6 +273,47 @@ int SUNBatchBDF_GB300_SetRefinementSweeps(SUNBatchBDF_GB300 b, int sweeps)
   return SUN_SUCCESS;
 }
 
+int SUNBatchBDF_GB300_SetPredictor(SUNBatchBDF_GB300 b, const uint16_t* d_weights,
+                                   const float* d_biases)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  if ((d_weights == nullptr) != (d_biases == nullptr)) return SUN_ERR_ARG_INCOMPATIBLE;
+  if (d_weights && !b->d_lp &&
+      !gb300::check_cuda(cudaMalloc(&b->d_lp, 2 * sizeof(unsigned long long)),
+                         "cudaMalloc(predictor counters)"))
+    return SUN_ERR_MEM_FAIL;
+  b->mlp_w = d_weights;
+  b->mlp_b = d_biases;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SetRecorder(SUNBatchBDF_GB300 b, uint16_t* d_x, float* d_t,
+                                  long long capacity, unsigned long long* d_count)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  if (d_x && (!d_t || !d_count || capacity < 0)) return SUN_ERR_ARG_INCOMPATIBLE;
+  b->rec_x     = d_x;
+  b->rec_t     = d_t;
+  b->rec_count = d_count;
+  b->rec_cap   = d_x ? capacity : 0;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_GetPredictorCounts(SUNBatchBDF_GB300 b, long long* calls, long long* kept)
+{
+  if (!b || !calls || !kept) return SUN_ERR_ARG_CORRUPT;
+  unsigned long long h[2] = {0, 0};
+  if (b->d_lp &&
+      !gb300::check_cuda(cudaMemcpyAsync(h, b->d_lp, sizeof h, cudaMemcpyDeviceToHost, b->stream),
+                         "cudaMemcpyAsync(predictor counters)"))
+    return SUN_ERR_EXT_FAIL;
+  if (!gb300::check_cuda(cudaStreamSynchronize(b->stream), "predictor counters"))
+    return SUN_ERR_EXT_FAIL;
+  *calls = (long long)h[0];
+  *kept  = (long long)h[1];
+  return SUN_SUCCESS;
+}
+
 int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
                                  double* d_yout, SUNBatchBDFStats* d_stats)
 {
@@ -284,8 +333,20 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.scratch = b->d_scratch;
   P.pivots  = b->d_piv;
   P.timers  = b->d_timers;
+  const bool fast = b->mode != SUNBATCHBDF_FP64_EXACT;  // the exact mode never uses them
+  P.mlp_w     = fast ? b->mlp_w : nullptr;
+  P.mlp_b     = fast ? b->mlp_b : nullptr;
+  P.lp_counts = (fast && b->mlp_w) ? b->d_lp : nullptr;
+  P.rec_x     = fast ? b->rec_x : nullptr;
+  P.rec_t     = b->rec_t;
+  P.rec_count = b->rec_count;
+  P.rec_cap   = b->rec_cap;
   if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 2 * sizeof(unsigned int), b->stream),
                          "cudaMemsetAsync(queue)"))
+    return SUN_ERR_EXT_FAIL;
+  if (P.lp_counts &&
+      !gb300::check_cuda(cudaMemsetAsync(b->d_lp, 0, 2 * sizeof(unsigned long long), b->stream),
+                         "cudaMemsetAsync(predictor counters)"))
     return SUN_ERR_EXT_FAIL;
   cudaEventRecord(b->ev0, b->stream);
   cudaError_t e = cudaSuccess;
@@ -367,6 +428,7 @@ void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b)
   cudaFree(b->d_scratch);
   cudaFree(b->d_piv);
   cudaFree(b->d_timers);
+  if (b->d_lp) cudaFree(b->d_lp);
   cudaEventDestroy(b->ev0);
   cudaEventDestroy(b->ev1);
   delete b;

@@ -29,6 +29,7 @@
 
 #include "../../include/sunbatchbdf_gb300.h"
 #include "ddpow.h"
+#include "mlp_device.cuh"
 
 namespace bdf {
 
@@ -104,6 +105,15 @@ struct Params
   double* scratch;         // per warp slot: SLOT_DOUBLES (saved Jacobian, FP64 LU)
   int* pivots;             // per warp slot: NMAX
   long long* timers;       // [slots][T_COUNT] when built with SUNGB300_BDF_TIMERS
+  // learned Newton predictor (fast modes; NULL = off)
+  const uint16_t* mlp_w;   // BF16 weights W1 | W2 | W3
+  const float* mlp_b;      // FP32 biases b1 | b2 | b3
+  unsigned long long* lp_counts;  // [0] predictor calls, [1] learned iterate kept
+  // training-data recorder (NULL = off): features and scaled converged correctors
+  uint16_t* rec_x;         // [cap][SUNMLP_IN_PAD] BF16
+  float* rec_t;            // [cap][64]
+  unsigned long long* rec_count;
+  long long rec_cap;
 };
 
 // Per-warp shared-memory slice for systems of at most NB species; the warp's
@@ -224,6 +234,8 @@ struct Integrator
   int q, qprime, qwait, L, indx_acor, nscon, convfail, qu;
   int nls_jcur, cv_jcur;
   long nst, nfe, nsetups, nje, nni, ncfn, netf, nnf, nstlp, nstlj;
+  long nlp, nlpu;  // learned predictor: calls, learned iterate kept
+  bool learned_start;  // the current Newton solve started from the learned iterate
 #ifdef SUNGB300_BDF_TIMERS
   long long tacc[T_COUNT] = {0};
 #endif
@@ -762,6 +774,56 @@ struct Integrator
     }
   }
 
+  // the same residual at ycor = 0 (the BDF predictor itself)
+  __device__ void nls_residual0(double* res)
+  {
+    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + 0.0;
+    rhs(w.y, w.ftemp);
+    const double a = -gamma;
+    for (int i = lane; i < n; i += 32)
+    {
+      double r = (rl1 * w.zn[1][i]) + 0.0;
+      res[i]   = r + a * w.ftemp[i];
+    }
+  }
+
+  // Predictor features (include/sunmlp_gb300.h) of the predicted state zn[0]:
+  // xr[c] = feature 32c + lane, rounded to BF16.
+  __device__ void mlp_features(float (&xr)[5])
+  {
+    using namespace gb300mlp;
+    double lam[2] = {0.0, 0.0};  // local consumption rates of species lane, lane + 32
+#pragma unroll
+    for (int h2 = 0; h2 < 2; ++h2)
+    {
+      const int j = lane + 32 * h2;
+      if (j < n)
+      {
+        double acc = 0.0;
+        for (int e = jptr[j]; e < jptr[j + 1]; e++)
+        {
+          const int ent = jent[e], r = ent >> 1;
+          if (rt[r] == 0) acc += rk[r];
+          else acc += rk[r] * w.zn[0][(ent & 1) ? ra[r] : rb[r]];
+        }
+        lam[h2] = acc;
+      }
+    }
+    const float fy0 = lane < n ? feat_y(w.zn[0][lane]) : 0.0f;
+    const float fy1 = lane + 32 < n ? feat_y(w.zn[0][lane + 32]) : 0.0f;
+    const float fr0 = lane < n ? feat_rate(gamma * lam[0]) : 0.0f;
+    const float fr1 = lane + 32 < n ? feat_rate(gamma * lam[1]) : 0.0f;
+    const float up0 = __shfl_up_sync(0xffffffffu, fr0, 1);
+    const float up1 = __shfl_up_sync(0xffffffffu, fr1, 1);
+    const float r31 = __shfl_sync(0xffffffffu, fr0, 31);
+    const float r63 = __shfl_sync(0xffffffffu, fr1, 31);
+    xr[0] = bf16_round(fy0);
+    xr[1] = bf16_round(fy1);
+    xr[2] = bf16_round(lane == 0 ? feat_gamma(gamma) : up0);  // 64: gamma; 65+i: species i
+    xr[3] = bf16_round(lane == 0 ? r31 : up1);                // species 31 + lane
+    xr[4] = bf16_round(lane == 0 ? r63 : 0.0f);               // species 63, then padding
+  }
+
   // cvNlsConvTest (cvode_nls.c:313)
   __device__ int nls_convtest(const double* ycor, double tol, int mcur)
   {
@@ -776,7 +838,8 @@ struct Integrator
     double dcon = del * (crate < 1.0 ? crate : 1.0) / tol;
     if (dcon <= 1.0)
     {
-      acnrm = (mcur == 0) ? del : wrms(ycor);
+      // ||ycor|| = ||delta|| after one iteration only when Newton started from 0
+      acnrm = (mcur == 0 && !learned_start) ? del : wrms(ycor);
       rv    = R_SUCCESS;
     }
     else if ((mcur >= 1) && (del > RDIV * delp)) rv = R_CONV_RECVR;
@@ -790,14 +853,16 @@ struct Integrator
   }
 
   // SUNNonlinSolSolve_Newton (sunnonlinsol_newton.c:179)
-  __device__ int newton_solve(double* ycor, double tol, int callLSetup)
+  // have_res: w.delta already holds the residual at ycor (first pass only).
+  __device__ int newton_solve(double* ycor, double tol, int callLSetup, bool have_res = false)
   {
     int jbad = 0, retval = R_SUCCESS;
     long niters = 0, nconvfails = 0;
     for (;;)
     {
       int curiter = 0;
-      nls_residual(ycor, w.delta);
+      if (!have_res) nls_residual(ycor, w.delta);
+      have_res = false;
       if (callLSetup)
       {
         retval = nls_lsetup(jbad);
@@ -830,8 +895,9 @@ struct Integrator
       if (retval > 0 && !nls_jcur)
       {
         nconvfails++;
-        callLSetup = 1;
-        jbad       = 1;
+        callLSetup    = 1;
+        jbad          = 1;
+        learned_start = false;
         for (int i = lane; i < n; i += 32) ycor[i] = 0.0;
         continue;
       }
@@ -1009,8 +1075,56 @@ struct Integrator
     int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
                     (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX_LSETUP);
     for (int i = lane; i < n; i += 32) w.acor[i] = 0.0;
-    int flag = newton_solve(w.acor, tq[4], callSetup);
+    bool have_res = false;
+    learned_start = false;
+    float xr[5];
+    const bool learn = !EXACT && (P.mlp_w != nullptr || P.rec_x != nullptr);
+    if (learn) mlp_features(xr);
+    if (!EXACT && P.mlp_w)
+    {
+      // learned initial iterate; kept only if its residual is the smaller
+      float o0, o1;
+      gb300mlp::warp_forward(P.mlp_w, P.mlp_b, xr, lane, o0, o1);
+      nlp++;
+      __syncwarp();
+      if (2 * lane < n) w.acor[2 * lane] = (double)(o0 / (float)w.ewt[2 * lane]);
+      if (2 * lane + 1 < n) w.acor[2 * lane + 1] = (double)(o1 / (float)w.ewt[2 * lane + 1]);
+      __syncwarp();
+      nls_residual(w.acor, w.delta);
+      const double rl = wrms(w.delta);
+      nls_residual0(w.tempv);
+      const double r0 = wrms(w.tempv);
+      learned_start = rl < r0;
+      if (learned_start) nlpu++;
+      else
+        for (int i = lane; i < n; i += 32)
+        {
+          w.acor[i]  = 0.0;
+          w.delta[i] = w.tempv[i];
+        }
+      __syncwarp();
+      have_res = true;
+    }
+    int flag = newton_solve(w.acor, tq[4], callSetup, have_res);
     if (flag != R_SUCCESS) return flag;
+    if (!EXACT && P.rec_x)
+    {
+      // training pair: features and the converged corrector in error-weight units
+      unsigned long long idx = 0;
+      if (lane == 0) idx = atomicAdd(P.rec_count, 1ull);
+      idx = __shfl_sync(0xffffffffu, idx, 0);
+      if ((long long)idx < P.rec_cap)
+      {
+        uint16_t* rx = P.rec_x + idx * gb300mlp::INP;
+        float* rtg   = P.rec_t + idx * gb300mlp::OUT;
+#pragma unroll
+        for (int c = 0; c < 5; ++c)
+          if (32 * c + lane < gb300mlp::INP)
+            rx[32 * c + lane] = __bfloat16_as_ushort(__float2bfloat16_rn(xr[c]));
+        for (int i = lane; i < gb300mlp::OUT; i += 32)
+          rtg[i] = i < n ? (float)(w.acor[i] * w.ewt[i]) : 0.0f;
+      }
+    }
     for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + w.acor[i];
     cv_jcur = 0;
     return R_SUCCESS;
@@ -1362,6 +1476,8 @@ struct Integrator
     nls_jcur = cv_jcur = 0;
     etamax = ETA_MAX_FS;
     nst = nfe = nsetups = nje = nni = ncfn = netf = nnf = nstlp = nstlj = 0;
+    nlp = nlpu    = 0;
+    learned_start = false;
     int istate = CV_SUCCESS;
     const double tout = P.tout;
 
@@ -1419,6 +1535,11 @@ struct Integrator
       st.tn      = tn;
       st.hu      = hu;
       P.stats[s] = st;
+    }
+    if (lane == 0 && P.lp_counts && nlp > 0)
+    {
+      atomicAdd(P.lp_counts, (unsigned long long)nlp);
+      atomicAdd(P.lp_counts + 1, (unsigned long long)nlpu);
     }
     __syncwarp();
   }

@@ -1,0 +1,96 @@
+"""The learned Newton predictor's pipeline: training data recorded by the plain
+FP64 integrator on the training seeds, training by the library's own BF16
+tensor-core kernels, and an A/B evaluation on held-out systems.
+
+Training data: every converged Newton solve of the plain solver on
+``generate(nsys, seed)`` for seeds 1001, 1002, ... (disjoint from the test
+seed 1) gives one row -- the solve's features and its converged corrector in
+error-weight units (include/sunbatchbdf_gb300.h, SetRecorder).  Targets are
+clipped to +-TARGET_CLIP weighted-RMS units: a guess that far off is never
+kept by the integrator's residual test anyway, and unclipped outliers would
+dominate the squared loss."""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from . import kinetics as K
+from .batch import BatchBDF
+from .mlp import MLP, IN_PAD, OUT
+
+TRAIN_SEED0 = 1001
+TARGET_CLIP = 16.0
+
+
+def record(nsys: int, seeds, capacity: int, rtol=1e-6, atol=1e-12, tout=100.0):
+    """(X, T) device tensors of recorded training rows (X: BF16 bits as int16)."""
+    import torch
+    X = torch.zeros((capacity, IN_PAD), dtype=torch.int16, device="cuda")
+    T = torch.zeros((capacity, OUT), dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int64, device="cuda")
+    for seed in seeds:
+        if int(cnt.item()) >= capacity:
+            break
+        B = BatchBDF(K.generate(nsys, seed=seed)).configure(rtol, atol, "fp64")
+        B.set_recorder(X.data_ptr(), T.data_ptr(), capacity, cnt.data_ptr())
+        B.solve(tout)
+        B.free()
+    n = min(int(cnt.item()), capacity)
+    return X[:n], T[:n].clamp_(-TARGET_CLIP, TARGET_CLIP)
+
+
+def train(mlp: MLP, X, T, epochs=8, batch=4096, lr=2e-3, seed=0):
+    """Adam over shuffled mini-batches (the last partial batch is dropped);
+    returns the loss of the last batch of each epoch."""
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    nb = X.shape[0] // batch
+    assert nb >= 1, "fewer rows than one batch"
+    losses = []
+    for _ in range(epochs):
+        perm = torch.randperm(X.shape[0], device="cuda", generator=gen)
+        loss = None
+        for b in range(nb):
+            idx = perm[b * batch:(b + 1) * batch]
+            xb = X.index_select(0, idx).contiguous()
+            tb = T.index_select(0, idx).contiguous()
+            loss = mlp.train_step(batch, xb.data_ptr(), tb.data_ptr(), lr, want_loss=(b == nb - 1))
+        losses.append(loss)
+    return losses
+
+
+def evaluate(batch: K.KineticsBatch, mlp: MLP, rtol=1e-6, atol=1e-12, tout=100.0, mode="mixed",
+             repeats=1):
+    """Solve the same systems with and without the predictor: counters,
+    kernel time, predictor usage and the final states."""
+    out = {}
+    for name, use in (("plain", False), ("learned", True)):
+        B = BatchBDF(batch).configure(rtol, atol, mode)
+        B.set_predictor(mlp if use else None)
+        ms = []
+        for _ in range(repeats):
+            y, st = B.solve(tout)
+            ms.append(B.last_kernel_ms)
+        res = {"kernel_ms": float(np.min(ms)), "y": y, "stats": st,
+               "nni": int(st["nni"].sum()), "nfe": int(st["nfe"].sum()),
+               "nst": int(st["nst"].sum()), "nsetups": int(st["nsetups"].sum()),
+               "ncfn": int(st["ncfn"].sum()), "failed": int(np.sum(st["flag"] != 0))}
+        if use:
+            res["calls"], res["kept"] = B.predictor_counts()
+        B.free()
+        out[name] = res
+    return out
+
+
+def pipeline(train_nsys=8192, seeds=4, capacity=1 << 20, epochs=8, mlp_seed=7):
+    """Record, train, return (mlp, info)."""
+    t0 = time.perf_counter()
+    X, T = record(train_nsys, range(TRAIN_SEED0, TRAIN_SEED0 + seeds), capacity)
+    t1 = time.perf_counter()
+    mlp = MLP(seed=mlp_seed)
+    losses = train(mlp, X, T, epochs=epochs)
+    t2 = time.perf_counter()
+    return mlp, {"rows": int(X.shape[0]), "record_s": t1 - t0, "train_s": t2 - t1,
+                 "losses": losses, "target_var": float(T.var().item())}
