@@ -127,7 +127,7 @@ struct WarpMem
   double rate[2 * NB];
   double red[NB];
   double rdiag[NB];
-  float fcol[NB];
+  float fcol[NB + 4];  // FP32 right-hand side of MIXED solves, zero-padded to the row stride
   int perm[NB];
 };
 
@@ -141,7 +141,7 @@ struct Layout
   static constexpr bool mat_in_smem  = (MODE == SUNBATCHBDF_MIXED);
   using MT = typename std::conditional<MODE == SUNBATCHBDF_MIXED, float, double>::type;
   static constexpr size_t mem_bytes  = (sizeof(WarpMem<NB>) + 15) / 16 * 16;
-  static constexpr size_t mat_bytes  = mat_in_smem ? sizeof(MT) * NB * (NB + 1) : 0;
+  static constexpr size_t mat_bytes  = mat_in_smem ? sizeof(MT) * NB * (NB + 4) : 0;
   static constexpr size_t warp_bytes = mem_bytes + mat_bytes;
   static constexpr int min_blocks    = mat_in_smem ? 8 : 12;
 };
@@ -198,12 +198,30 @@ __device__ __forceinline__ long long abs_key(float v)
 __device__ __forceinline__ bool is_zero(double v) { return (__double_as_longlong(v) << 1) == 0; }
 __device__ __forceinline__ bool is_zero(float v) { return (__float_as_int(v) << 1) == 0; }
 
-// SUNRpowerR: the exact mode rounds pow correctly (double-double), the fast
-// modes use the device pow.
-template <bool EXACT>
-__device__ __forceinline__ double cv_pow(double x, double y)
+// x^(1/k), k = 1..7, for the fast modes: an FP32 estimate 2^(log2(x)/k)
+// refined by one Newton step y <- y - (y^k - x) / (k y^(k-1)) whose residual
+// y^k - x is formed in FP64 (the step only needs its divisor to FP32
+// accuracy).  From a ~2^-21 estimate the step leaves a relative error below
+// 1e-13, at about k + 4 FP64 instructions instead of a full FP64 pow.
+__device__ __forceinline__ double fast_root(double x, int k)
 {
-  return EXACT ? dd_pow(x, y) : pow(x, y);
+  if (k == 1) return x;
+  if (!(x >= 1e-36 && x <= 1e36)) return x == 0.0 ? 0.0 : pow(x, 1.0 / k);
+  const float yf = exp2f(__log2f((float)x) / (float)k);
+  const double y = (double)yf;
+  double pk1     = y;
+  for (int i = 2; i < k; i++) pk1 *= y;  // y^(k-1)
+  const double d   = pk1 * y - x;
+  const float rdiv = 1.0f / ((float)k * (float)pk1);
+  return y - d * (double)rdiv;
+}
+
+// SUNRpowerR(x, 1/k) of the step-size controller: the exact mode rounds it
+// correctly (double-double), the fast modes use fast_root.
+template <bool EXACT>
+__device__ __forceinline__ double cv_root(double x, int k)
+{
+  return EXACT ? dd_pow(x, inv_int(k)) : fast_root(x, k);
 }
 
 template <int MODE, int NB>
@@ -225,7 +243,9 @@ struct Integrator
   double* J;   // saved Jacobian, column-major n x n (global memory)
   double* M;   // Newton matrix / its LU factors (FP64 modes; shared memory)
   float* M32;  // Newton matrix / its inverse (MIXED; shared memory)
-  int ld;      // leading dimension of M / M32 (odd)
+  float* J32;  // FP32 copy of J (MIXED; global scratch after J)
+  int ld;      // leading dimension of M (FP64 modes, column-major, odd)
+  int lr;      // row stride of M32 (MIXED, row-major): a multiple of 4, lr/4 odd
   int* piv;
   // CVODE state (identical in every lane)
   double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu;
@@ -348,6 +368,15 @@ struct Integrator
       }
     }
     __syncwarp();
+    if (MIXED)
+    {  // row-major FP32 copy the Newton matrices are built from until the next J
+      for (int e = lane; e < n * n; e += 32)
+      {
+        const int j = e / n, i = e - j * n;
+        J32[i * n + j] = (float)J[e];
+      }
+      __syncwarp();
+    }
     BDF_TOC(t0, T_JAC);
   }
 
@@ -440,27 +469,40 @@ struct Integrator
   // from every other row (the pivot column then holds -a_ik/pivot), and the
   // row interchanges are undone on the columns at the end, in reverse order.
   // The pivot choice is the LU factorisation's.  Returns 0 or k+1.
+  // In-place Gauss-Jordan inversion with partial pivoting of the FP32 matrix
+  // (row-major, row stride lr, padding columns zero); returns 0 or k+1 for a
+  // zero pivot in column k.  Lane l owns rows l and l + 32; every row update
+  // moves 16-byte chunks (the stride makes 8 consecutive rows' chunks fall in
+  // distinct bank quads), so an FMA costs well under one memory instruction.
   __device__ int gauss_jordan(float* a)
   {
+    const int nq   = lr >> 2;
+    float4* A4     = reinterpret_cast<float4*>(a);
+    const int i0   = lane, i1 = lane + 32;
+    const bool h0  = i0 < n, h1 = two && i1 < n;
     for (int k = 0; k < n; k++)
     {
-      float* ck    = a + k * ld;
       long long bk = -1;
       int bi       = n;
-      for (int i = k + lane; i < n; i += 32)
+      if (h0 && i0 >= k)
       {
-        long long v = abs_key(ck[i]);
+        bk = abs_key(a[i0 * lr + k]);
+        bi = i0;
+      }
+      if (h1 && i1 >= k)
+      {
+        const long long v = abs_key(a[i1 * lr + k]);
         if (v > bk)
         {
           bk = v;
-          bi = i;
+          bi = i1;
         }
       }
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1)
       {
-        long long ov = __shfl_xor_sync(0xffffffffu, bk, off);
-        int oi       = __shfl_xor_sync(0xffffffffu, bi, off);
+        const long long ov = __shfl_xor_sync(0xffffffffu, bk, off);
+        const int oi       = __shfl_xor_sync(0xffffffffu, bi, off);
         if (ov > bk || (ov == bk && oi < bi))
         {
           bk = ov;
@@ -471,103 +513,133 @@ struct Integrator
       const int l = bi;
       if (lane == 0) w.perm[k] = l;
       if (l != k)
-        for (int j = lane; j < n; j += 32)
+        for (int c = lane; c < nq; c += 32)
         {
-          float t       = a[j * ld + l];
-          a[j * ld + l] = a[j * ld + k];
-          a[j * ld + k] = t;
+          const float4 t  = A4[k * nq + c];
+          A4[k * nq + c] = A4[l * nq + c];
+          A4[l * nq + c] = t;
         }
       __syncwarp();
-      const float rp = 1.f / ck[k];
-      // each lane owns rows i0 = lane, i1 = lane + 32; f = old a[k][i]
-      const int i0 = lane, i1 = lane + 32;
-      const float f0 = (i0 < n) ? ck[i0] : 0.f;
-      const float f1 = (two && i1 < n) ? ck[i1] : 0.f;
+      const float rp = 1.f / a[k * lr + k];
       __syncwarp();
-      for (int j = lane; j < n; j += 32) a[j * ld + k] = (j == k ? 1.f : a[j * ld + k]) * rp;
+      if (lane == 0) a[k * lr + k] = 1.f;  // the pivot position becomes rp
       __syncwarp();
-      // every other row: a[j][i] -= f_i * a[j][k] (row k entry broadcast);
-      // column k becomes -f_i * rp.  Four columns per trip.
-      const bool own0 = i0 < n && i0 != k, own1 = two && i1 < n && i1 != k;
-      int j = 0;
-      for (; j + 4 <= n; j += 4)
+      for (int c = lane; c < nq; c += 32)
       {
-        float rk[4], v0[4], v1[4];
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-        {
-          rk[u] = a[(j + u) * ld + k];
-          v0[u] = own0 ? a[(j + u) * ld + i0] : 0.f;
-          v1[u] = own1 ? a[(j + u) * ld + i1] : 0.f;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-        {
-          const bool pc = (j + u) == k;
-          if (own0) a[(j + u) * ld + i0] = pc ? -f0 * rp : fmaf(-f0, rk[u], v0[u]);
-          if (own1) a[(j + u) * ld + i1] = pc ? -f1 * rp : fmaf(-f1, rk[u], v1[u]);
-        }
+        float4 v = A4[k * nq + c];
+        v.x *= rp;
+        v.y *= rp;
+        v.z *= rp;
+        v.w *= rp;
+        A4[k * nq + c] = v;
       }
-      for (; j < n; j++)
-      {
-        const float rk = a[j * ld + k];
-        const bool pc  = j == k;
-        if (own0) a[j * ld + i0] = pc ? -f0 * rp : fmaf(-f0, rk, a[j * ld + i0]);
-        if (own1) a[j * ld + i1] = pc ? -f1 * rp : fmaf(-f1, rk, a[j * ld + i1]);
-      }
+      __syncwarp();
+      // rows i != k: a[i][:] -= a[i][k] * a[k][:], with a[i][k] first set to 0
+      // (so it ends as -a[i][k] * rp)
+      const bool e0 = h0 && i0 != k, e1 = h1 && i1 != k;
+      const float f0 = e0 ? a[i0 * lr + k] : 0.f;
+      const float f1 = e1 ? a[i1 * lr + k] : 0.f;
+      if (e0) a[i0 * lr + k] = 0.f;
+      if (e1) a[i1 * lr + k] = 0.f;
+      if (e0 || e1)
+        for (int c0 = 0; c0 < nq; c0 += 4)
+        {
+          // four chunks' loads issued before any store (row k is never
+          // written here, but the compiler cannot prove it)
+          float4 y[4], x0[4], x1[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+          {
+            const int c = c0 + u < nq ? c0 + u : nq - 1;
+            y[u]        = A4[k * nq + c];
+            x0[u]       = e0 ? A4[i0 * nq + c] : y[u];
+            x1[u]       = e1 ? A4[i1 * nq + c] : y[u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+          {
+            x0[u].x = fmaf(-f0, y[u].x, x0[u].x);
+            x0[u].y = fmaf(-f0, y[u].y, x0[u].y);
+            x0[u].z = fmaf(-f0, y[u].z, x0[u].z);
+            x0[u].w = fmaf(-f0, y[u].w, x0[u].w);
+            x1[u].x = fmaf(-f1, y[u].x, x1[u].x);
+            x1[u].y = fmaf(-f1, y[u].y, x1[u].y);
+            x1[u].z = fmaf(-f1, y[u].z, x1[u].z);
+            x1[u].w = fmaf(-f1, y[u].w, x1[u].w);
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (c0 + u < nq)
+            {
+              if (e0) A4[i0 * nq + c0 + u] = x0[u];
+              if (e1) A4[i1 * nq + c0 + u] = x1[u];
+            }
+        }
       __syncwarp();
     }
+    // undo the row interchanges as column interchanges, last first
     for (int k = n - 1; k >= 0; k--)
     {
       const int p = w.perm[k];
       if (p != k)
-        for (int i = lane; i < n; i += 32)
+      {
+        if (h0)
         {
-          float t       = a[k * ld + i];
-          a[k * ld + i] = a[p * ld + i];
-          a[p * ld + i] = t;
+          const float t    = a[i0 * lr + k];
+          a[i0 * lr + k] = a[i0 * lr + p];
+          a[i0 * lr + p] = t;
         }
-      __syncwarp();
+        if (h1)
+        {
+          const float t    = a[i1 * lr + k];
+          a[i1 * lr + k] = a[i1 * lr + p];
+          a[i1 * lr + p] = t;
+        }
+      }
     }
+    __syncwarp();
     return 0;
   }
 
   // x = A b for a column-major FP32 matrix (leading dimension ld); b, x in
   // registers; four columns per trip, two accumulators per element.
+  // x = A b for the FP32 inverse (row-major, stride lr): b goes through
+  // w.fcol (zero-padded to lr), each lane forms the dot products of its rows
+  // with 16-byte loads and four partial sums.
   __device__ void matvec32(const float* A, float b0, float b1, float& x0, float& x1)
   {
-    float a0 = 0.f, a1 = 0.f, c0 = 0.f, c1 = 0.f;
-    int j = 0;
-    for (; j + 4 <= n; j += 4)
+    if (lane < n) w.fcol[lane] = b0;
+    if (lane + 32 < n) w.fcol[lane + 32] = b1;
+    for (int i = n + lane; i < lr; i += 32) w.fcol[i] = 0.f;
+    __syncwarp();
+    const int nq      = lr >> 2;
+    const float4* A4  = reinterpret_cast<const float4*>(A);
+    const float4* B4  = reinterpret_cast<const float4*>(w.fcol);
+    const bool h0 = lane < n, h1 = two && lane + 32 < n;
+    float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0;
+    for (int c = 0; c < nq; c++)
     {
-      float bj[4], v0[4], v1[4];
-#pragma unroll
-      for (int u = 0; u < 4; u++)
+      const float4 bj = B4[c];
+      if (h0)
       {
-        bj[u] = __shfl_sync(0xffffffffu, (j + u) < 32 ? b0 : b1, (j + u) & 31);
-        v0[u] = lane < n ? A[(j + u) * ld + lane] : 0.f;
-        v1[u] = (two && lane + 32 < n) ? A[(j + u) * ld + lane + 32] : 0.f;
+        const float4 v = A4[lane * nq + c];
+        s0.x = fmaf(v.x, bj.x, s0.x);
+        s0.y = fmaf(v.y, bj.y, s0.y);
+        s0.z = fmaf(v.z, bj.z, s0.z);
+        s0.w = fmaf(v.w, bj.w, s0.w);
       }
-      a0 = fmaf(v0[0], bj[0], a0);
-      c0 = fmaf(v0[1], bj[1], c0);
-      a0 = fmaf(v0[2], bj[2], a0);
-      c0 = fmaf(v0[3], bj[3], c0);
-      if (two)
+      if (h1)
       {
-        a1 = fmaf(v1[0], bj[0], a1);
-        c1 = fmaf(v1[1], bj[1], c1);
-        a1 = fmaf(v1[2], bj[2], a1);
-        c1 = fmaf(v1[3], bj[3], c1);
+        const float4 v = A4[(lane + 32) * nq + c];
+        s1.x = fmaf(v.x, bj.x, s1.x);
+        s1.y = fmaf(v.y, bj.y, s1.y);
+        s1.z = fmaf(v.z, bj.z, s1.z);
+        s1.w = fmaf(v.w, bj.w, s1.w);
       }
     }
-    for (; j < n; j++)
-    {
-      const float bj = __shfl_sync(0xffffffffu, j < 32 ? b0 : b1, j & 31);
-      if (lane < n) a0 = fmaf(A[j * ld + lane], bj, a0);
-      if (two && lane + 32 < n) a1 = fmaf(A[j * ld + lane + 32], bj, a1);
-    }
-    x0 = a0 + c0;
-    x1 = a1 + c1;
+    __syncwarp();
+    x0 = (s0.x + s0.y) + (s0.z + s0.w);
+    x1 = (s1.x + s1.y) + (s1.z + s1.w);
   }
 
   // y = J x with the saved FP64 Jacobian in global memory (column-major,
@@ -680,14 +752,13 @@ struct Integrator
     const double c = -gamma;
     int lu;
     if (MIXED)
-    {
-      for (int e = lane; e < n * n; e += 32)
+    {  // M = I - gamma J in FP32 (row-major, zero padding columns), then its inverse
+      const float cf = (float)c;
+      for (int e = lane; e < n * lr; e += 32)
       {
-        const int j = e / n, i = e - j * n;
-        M32[j * ld + i] = (float)(J[e] * c);
+        const int i = e / lr, j = e - i * lr;
+        M32[e] = j < n ? J32[i * n + j] * cf + (i == j ? 1.0f : 0.0f) : 0.0f;
       }
-      __syncwarp();
-      for (int i = lane; i < n; i += 32) M32[i * ld + i] = (float)(J[i * n + i] * c + 1.0);
       __syncwarp();
       lu = gauss_jordan(M32);
     }
@@ -1058,9 +1129,102 @@ struct Integrator
     set_tq_bdf(hsum, alpha0, alpha0_hat, xi_inv, xistar_inv);
   }
 
+  // cvSetBDF + cvSetTqBDF with their independent divisions spread over
+  // lanes (fast modes): every quotient has the same operands and rounding as
+  // in set_bdf / set_tq_bdf, but each round of divisions costs one warp
+  // instruction sequence instead of one per quotient.
+  __device__ void set_bdf_lanes()
+  {
+    // hsum_m = h + tau[1] + ... + tau[m-1] (the reference's summation order),
+    // xi_inv_m = h / hsum_m for m = 2 .. q+1, on lane m
+    double hs = h, my_hsum = h;
+    for (int m = 2; m <= q + 1; m++)
+    {
+      hs += tau[m - 1];
+      if (lane == m) my_hsum = hs;
+    }
+    const double my_xi = h / my_hsum;
+    // l[i] on lane i: l[0] = l[1] = 1, then for j = 2..q-1 l[i] += l[i-1] * xi_inv_j
+    double li = (lane <= 1) ? 1.0 : 0.0;
+    double alpha0 = -1.0, alpha0_hat = -1.0, xi_inv = 1.0, xistar_inv = 1.0, hsum = h;
+    if (q > 1)
+    {
+      for (int j = 2; j < q; j++)
+      {
+        hsum += tau[j - 1];
+        xi_inv = __shfl_sync(0xffffffffu, my_xi, j);
+        alpha0 -= inv_int(j);
+        const double lm1 = __shfl_up_sync(0xffffffffu, li, 1);
+        if (lane >= 1 && lane <= j) li += lm1 * xi_inv;
+      }
+      alpha0 -= inv_int(q);
+      const double l1 = __shfl_sync(0xffffffffu, li, 1);
+      xistar_inv      = -l1 - alpha0;
+      hsum += tau[q - 1];
+      xi_inv     = __shfl_sync(0xffffffffu, my_xi, q);
+      alpha0_hat = -l1 - xi_inv;
+      const double lm1 = __shfl_up_sync(0xffffffffu, li, 1);
+      if (lane >= 1 && lane <= q) li += lm1 * xistar_inv;
+    }
+#pragma unroll
+    for (int i = 0; i <= QMAX; i++) l[i] = __shfl_sync(0xffffffffu, li, i);
+    // cvSetTqBDF: first round of quotients
+    const double A1  = 1.0 - alpha0_hat + alpha0;
+    const double A2  = 1.0 + q * A1;
+    const double A3  = alpha0 + inv_int(q);
+    const double A4  = alpha0_hat + xi_inv;
+    const double xq1 = __shfl_sync(0xffffffffu, my_xi, q + 1);  // h / (hsum + tau[q])
+    const double A5  = alpha0 - inv_int(q + 1);
+    const double A6  = alpha0_hat - xq1;
+    double num = 1.0, den = 1.0;
+    switch (lane)
+    {
+    case 0: num = A1; den = alpha0 * A2; break;                    // tq[2]
+    case 1: num = A2 * xistar_inv; den = l[q] * xi_inv; break;     // tq[5]
+    case 2: num = xistar_inv; den = l[q]; break;                   // C
+    case 3: num = 1.0 - A4 + A3; den = A3; break;                  // Cpinv
+    case 4: num = 1.0 - A6 + A5; den = A2; break;                  // Cppinv
+    case 5: num = 1.0; den = l[1]; break;                          // rl1
+    default: break;
+    }
+    const double qt    = num / den;
+    tq[2]              = fabs(__shfl_sync(0xffffffffu, qt, 0));
+    tq[5]              = fabs(__shfl_sync(0xffffffffu, qt, 1));
+    const double C     = __shfl_sync(0xffffffffu, qt, 2);
+    const double Cpinv = __shfl_sync(0xffffffffu, qt, 3);
+    const double Cpp   = __shfl_sync(0xffffffffu, qt, 4);
+    rl1                = __shfl_sync(0xffffffffu, qt, 5);
+    gamma              = h * rl1;
+    if (nst == 0) gammap = gamma;
+    // second round: tq[4], tq[3], gamrat
+    num = 1.0;
+    den = 1.0;
+    switch (lane)
+    {
+    case 0: num = CORTES; den = tq[2]; break;
+    case 1: num = Cpp; den = xq1 * (q + 2) * A5; break;
+    case 2: num = gamma; den = gammap; break;
+    default: break;
+    }
+    const double qt2 = num / den;
+    tq[4]            = __shfl_sync(0xffffffffu, qt2, 0);
+    if (qwait == 1)
+    {
+      tq[1] = (q > 1) ? fabs(C * Cpinv) : 1.0;
+      tq[3] = fabs(__shfl_sync(0xffffffffu, qt2, 1));
+    }
+    gamrat = (nst > 0) ? __shfl_sync(0xffffffffu, qt2, 2) : 1.0;
+  }
+
   __device__ void set_coeffs()
   {  // cvSet (cvode.c:2791)
     BDF_TIC(t0);
+    if (!EXACT)
+    {
+      set_bdf_lanes();
+      BDF_TOC(t0, T_SETC);
+      return;
+    }
     set_bdf();
     rl1   = 1.0 / l[1];
     gamma = h * rl1;
@@ -1158,7 +1322,7 @@ struct Integrator
     etamax = 1.0;
     if (*nefPtr <= MXNEF1)
     {
-      eta = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, inv_int(L)) + ADDON);
+      eta = 1.0 / (cv_root<EXACT>(BIAS2 * dsm, L) + ADDON);
       eta = dmax(ETA_MIN_EF, dmax(eta, 0.0));
       if (*nefPtr >= SMALL_NEF) eta = dmin(eta, ETA_MAX_EF);
       rescale();
@@ -1238,7 +1402,7 @@ struct Integrator
     if (q > 1)
     {
       double ddn = wrms(w.zn[q]) * tq[1];
-      etaqm1     = 1.0 / (cv_pow<EXACT>(BIAS1 * ddn, inv_int(q)) + ADDON);
+      etaqm1     = 1.0 / (cv_root<EXACT>(BIAS1 * ddn, q) + ADDON);
     }
     return etaqm1;
   }
@@ -1255,7 +1419,7 @@ struct Integrator
       const double a = -cquot;
       for (int i = lane; i < n; i += 32) w.tempv[i] = (a * w.zn[QMAX][i]) + w.acor[i];
       double dup = wrms(w.tempv) * tq[3];
-      etaqp1     = 1.0 / (cv_pow<EXACT>(BIAS3 * dup, inv_int(L + 1)) + ADDON);
+      etaqp1     = 1.0 / (cv_root<EXACT>(BIAS3 * dup, L + 1) + ADDON);
     }
     return etaqp1;
   }
@@ -1296,7 +1460,7 @@ struct Integrator
       eta    = 1.0;
       return;
     }
-    etaq = 1.0 / (cv_pow<EXACT>(BIAS2 * dsm, inv_int(L)) + ADDON);
+    etaq = 1.0 / (cv_root<EXACT>(BIAS2 * dsm, L) + ADDON);
     if (qwait != 0)
     {
       eta    = etaq;
@@ -1454,7 +1618,10 @@ struct Integrator
     jptr = p.jptr + p.y_off[s] + s;
     jent = p.jent + p.je_off[s];
     J     = scratch;
+    J32   = (float*)(scratch + SLOT_J);
     ld    = n | 1;
+    lr    = (n + 3) & ~3;
+    if (((lr >> 2) & 1) == 0) lr += 4;
     piv   = pivbuf;
     rdiag = w.rdiag;
     two   = n > 32;
