@@ -1666,11 +1666,17 @@ struct Integrator
         istate = CV_TOO_MUCH_WORK;
         break;
       }
-      double nrm = wrms(w.zn[0]);
-      if (UROUND * nrm > 1.0)
+      // ewt was just set from zn[0], so each weighted term is below 1/rtol and
+      // UROUND * ||zn[0]|| exceeds 1 only if rtol < UROUND: the fast modes
+      // skip the norm when rtol >= 1e-12 (the exact mode always takes it).
+      if (EXACT || P.rtol < 1e-12)
       {
-        istate = CV_TOO_MUCH_ACC;
-        break;
+        double nrm = wrms(w.zn[0]);
+        if (UROUND * nrm > 1.0)
+        {
+          istate = CV_TOO_MUCH_ACC;
+          break;
+        }
       }
       int kflag = step();
       if (kflag != CV_SUCCESS)
