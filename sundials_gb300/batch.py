@@ -122,3 +122,29 @@ class BatchBDF:
             self.free()
         except Exception:
             pass
+
+
+def _main(argv=None):
+    """One solve of the seeded kinetics batch (a profiling and smoke entry):
+    python -m sundials_gb300.batch --nsys 4096 --mode mixed"""
+    import argparse
+    import json
+
+    from . import kinetics as K
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nsys", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--mode", choices=sorted(MODES), default="mixed")
+    ap.add_argument("--rtol", type=float, default=1e-6)
+    ap.add_argument("--atol", type=float, default=1e-12)
+    ap.add_argument("--tout", type=float, default=100.0)
+    args = ap.parse_args(argv)
+    b = BatchBDF(K.generate(args.nsys, seed=args.seed)).configure(args.rtol, args.atol, args.mode)
+    _, st = b.solve(args.tout)
+    print(json.dumps({"nsys": args.nsys, "mode": args.mode, "kernel_ms": round(b.last_kernel_ms, 3),
+                      "nst": int(st["nst"].sum()), "nni": int(st["nni"].sum()),
+                      "nsetups": int(st["nsetups"].sum()), "failed": int((st["flag"] != 0).sum())}))
+
+
+if __name__ == "__main__":
+    _main()
