@@ -446,7 +446,7 @@ def run_kinetics(args, world, rank, local):
     # weak scaling: every rank integrates its own 65,536-system batch
     nsys = args.nsys
     batch = K.generate(nsys, seed=1 + rank * 1000003 if rank else 1)
-    stats_bytes = 96 * nsys
+    stats_bytes = K.BATCH_STATS_DTYPE.itemsize * nsys
     d_y0 = torch.from_numpy(batch.y0.copy()).cuda()
     d_yout = torch.zeros_like(d_y0)
     d_stats = torch.zeros(stats_bytes, dtype=torch.uint8, device="cuda")
@@ -465,7 +465,7 @@ def run_kinetics(args, world, rank, local):
     elapsed = max_over_ranks(world, float(np.sum(times)))
     value = nsys * args.steps * world / elapsed
     yout_mixed = d_yout.cpu().numpy()
-    st = np.frombuffer(d_stats.cpu().numpy().tobytes(), K.STATS_DTYPE)
+    st = np.frombuffer(d_stats.cpu().numpy().tobytes(), K.BATCH_STATS_DTYPE)
 
     # ---- e2e through the C ABI with host buffers (H2D y0, solve, D2H y, stats)
     e2e_steps = max(1, min(args.steps, 3))

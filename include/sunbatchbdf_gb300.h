@@ -37,6 +37,7 @@
 #define SUNBATCHBDF_GB300_H
 
 #include <stdint.h>
+#include <stdio.h>
 
 #include "sundials_gb300_abi.h"
 
@@ -77,6 +78,9 @@ typedef struct
   int64_t qu;   /* last order used */
   double tn;    /* internal time reached */
   double hu;    /* last step size used */
+  double h0u;   /* initial step size used (CVodeGetActualInitStep) */
+  double next_h;   /* step size to be attempted next (CVodeGetCurrentStep) */
+  int64_t next_q;  /* order to be attempted next (CVodeGetCurrentOrder) */
 } SUNBatchBDFStats;
 
 typedef struct SUNBatchBDF_GB300_* SUNBatchBDF_GB300;
@@ -108,6 +112,17 @@ SUNGB300_EXPORT int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0,
 
 /* Wall time of the last Solve's integration kernel in milliseconds. */
 SUNGB300_EXPORT double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b);
+
+/* Statistics of system `sys` (host array from Solve) in the layout of
+ * CVodePrintAllStats (src/cvode/cvode_io.c:1626): the same names, order and
+ * number formats, fmt 0 = SUN_OUTPUTFORMAT_TABLE, 1 = SUN_OUTPUTFORMAT_CSV; the
+ * linear-solver lines are those of CVODE with SUNLINSOL_DENSE and an analytic
+ * Jacobian (no preconditioner, no Krylov iterations, no difference-quotient
+ * RHS calls); no root finding, no projection.  Returns 0, or
+ * SUN_ERR_ARG_OUTOFRANGE for a bad format or system index. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_PrintAllStats(const SUNBatchBDFStats* stats,
+                                                    int64_t nsys, int64_t sys, FILE* outfile,
+                                                    int fmt);
 
 /* Learned Newton predictor (include/sunmlp_gb300.h; no counterpart in the
  * reference).  With device weights set, every Newton solve of the fast modes

@@ -6,7 +6,7 @@ import ctypes as ct
 import numpy as np
 
 from . import _lib
-from .kinetics import STATS_DTYPE, KineticsBatch
+from .kinetics import BATCH_STATS_DTYPE, KineticsBatch
 
 FP64, FP64_EXACT, MIXED = 0, 1, 2
 MODES = {"fp64": FP64, "fp64_exact": FP64_EXACT, "mixed": MIXED}
@@ -72,7 +72,7 @@ class BatchBDF:
     def solve(self, tout=100.0, t0=0.0, y0=None):
         y0 = np.ascontiguousarray(self.batch.y0 if y0 is None else y0, np.float64)
         yout = np.zeros_like(y0)
-        stats = np.zeros(self.batch.nsys, STATS_DTYPE)
+        stats = np.zeros(self.batch.nsys, BATCH_STATS_DTYPE)
         rc = self.lib.SUNBatchBDF_GB300_Solve(self.h, t0, y0.ctypes.data, tout,
                                               yout.ctypes.data, stats.ctypes.data)
         if rc != 0:

@@ -403,6 +403,68 @@ int SUNBatchBDF_GB300_Solve(SUNBatchBDF_GB300 b, double t0, const double* y0, do
 
 double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b) { return b ? b->last_ms : 0.0; }
 
+// CVodePrintAllStats (src/cvode/cvode_io.c:1626) for one system of the batch:
+// sunfprintf_real / sunfprintf_long (src/sundials/sundials_utils.h:89-117)
+// with a 29-character name column and DBL_DIG significant digits.
+int SUNBatchBDF_GB300_PrintAllStats(const SUNBatchBDFStats* stats, int64_t nsys, int64_t sys,
+                                    FILE* out, int fmt)
+{
+  if (!stats || !out || sys < 0 || sys >= nsys || (fmt != 0 && fmt != 1))
+    return SUN_ERR_ARG_OUTOFRANGE;
+  const SUNBatchBDFStats& st = stats[sys];
+  bool start = true;
+  auto real = [&](const char* name, double v) {
+    if (fmt == 0) fprintf(out, "%-29s = %.15g\n", name, v);
+    else
+    {
+      if (!start) fprintf(out, ",");
+      fprintf(out, "%s,% .15e", name, v);
+    }
+    start = false;
+  };
+  auto lng = [&](const char* name, long v) {
+    if (fmt == 0) fprintf(out, "%-29s = %ld\n", name, v);
+    else
+    {
+      if (!start) fprintf(out, ",");
+      fprintf(out, "%s,%ld", name, v);
+    }
+    start = false;
+  };
+  real("Current time", st.tn);
+  lng("Steps", (long)st.nst);
+  lng("Error test fails", (long)st.netf);
+  lng("NLS step fails", (long)st.ncfn);
+  real("Initial step size", st.h0u);
+  real("Last step size", st.hu);
+  real("Current step size", st.next_h);
+  lng("Last method order", (long)st.qu);
+  lng("Current method order", (long)st.next_q);
+  lng("Stab. lim. order reductions", 0L);
+  lng("RHS fn evals", (long)st.nfe);
+  lng("NLS iters", (long)st.nni);
+  lng("NLS fails", (long)st.nnf);
+  if (st.nst > 0) real("NLS iters per step", (double)st.nni / (double)st.nst);
+  lng("LS setups", (long)st.nsetups);
+  // SUNLINSOL_DENSE with an analytic Jacobian
+  lng("Jac fn evals", (long)st.nje);
+  lng("LS RHS fn evals", 0L);
+  lng("Prec setup evals", 0L);
+  lng("Prec solves", 0L);
+  lng("LS iters", 0L);
+  lng("LS fails", 0L);
+  lng("Jac-times setups", 0L);
+  lng("Jac-times evals", 0L);
+  if (st.nni > 0)
+  {
+    real("LS iters per NLS iter", 0.0 / (double)st.nni);
+    real("Jac evals per NLS iter", (double)st.nje / (double)st.nni);
+    real("Prec evals per NLS iter", 0.0 / (double)st.nni);
+  }
+  lng("Root fn evals", 0L);
+  return SUN_SUCCESS;
+}
+
 #ifdef SUNGB300_BDF_TIMERS
 // Section cycle totals summed over warp slots (instrumented builds only).
 SUNGB300_EXPORT int SUNBatchBDF_GB300_SectionCycles(SUNBatchBDF_GB300 b, long long* out)

@@ -248,7 +248,8 @@ struct Integrator
   int lr;      // row stride of M32 (MIXED, row-major): a multiple of 4, lr/4 odd
   int* piv;
   // CVODE state (identical in every lane)
-  double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu;
+  double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu, h0u;
+  int next_q;
   double saved_tq5, rl1, gamma, gammap, gamrat, crate, delp, acnrm;
   double tq[6], l[QMAX + 2], tau[QMAX + 2];
   int q, qprime, qwait, L, indx_acor, nscon, convfail, qu;
@@ -1630,7 +1631,8 @@ struct Integrator
     const double* y0 = P.y0 + p.y_off[s];
     for (int i = lane; i < n; i += 32) w.zn[0][i] = y0[i];
     tn = P.t0;
-    h = hscale = hprime = next_h = eta = etaq = etaqm1 = etaqp1 = hu = 0.0;
+    h = hscale = hprime = next_h = eta = etaq = etaqm1 = etaqp1 = hu = h0u = 0.0;
+    next_q = 0;
     saved_tq5 = rl1 = gamma = gammap = gamrat = crate = delp = acnrm = 0.0;
     for (int i = 0; i < 6; i++) tq[i] = 0.0;
     for (int i = 0; i < QMAX + 2; i++) l[i] = tau[i] = 0.0;
@@ -1653,6 +1655,7 @@ struct Integrator
     hin(tout);
     hscale = h;
     hprime = h;
+    h0u    = h;
     for (int i = lane; i < n; i += 32) w.zn[1][i] *= h;
 
     long nstloc = 0;
@@ -1660,6 +1663,7 @@ struct Integrator
     for (;;)
     {
       next_h = h;
+      next_q = q;
       if (nst > 0) set_ewt(w.zn[0], w.ewt);
       if ((P.mxstep > 0) && (nstloc >= P.mxstep))
       {
@@ -1685,7 +1689,12 @@ struct Integrator
         break;
       }
       nstloc++;
-      if ((tn - tout) * h >= 0.0) break;
+      if ((tn - tout) * h >= 0.0)
+      {
+        next_q = qprime;
+        next_h = hprime;
+        break;
+      }
     }
     BDF_TOC(tall, T_OTHER);
     double* yo = P.yout + p.y_off[s];
@@ -1707,6 +1716,9 @@ struct Integrator
       st.qu      = qu;
       st.tn      = tn;
       st.hu      = hu;
+      st.h0u     = h0u;
+      st.next_h  = next_h;
+      st.next_q  = next_q;
       P.stats[s] = st;
     }
     if (lane == 0 && P.lp_counts && nlp > 0)

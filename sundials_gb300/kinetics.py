@@ -138,6 +138,10 @@ def rhs(batch: KineticsBatch, i: int, y: np.ndarray) -> np.ndarray:
 # ------------------------------------------------------------- file format
 STATS_FIELDS = ["nst", "nfe", "nsetups", "nje", "nni", "ncfn", "netf", "nnf", "flag", "qu"]
 STATS_DTYPE = np.dtype([(f, "<i8") for f in STATS_FIELDS] + [("tn", "<f8"), ("hu", "<f8")])
+# SUNBatchBDFStats (include/sunbatchbdf_gb300.h): the drivers' fields plus the
+# three CVodePrintAllStats needs
+BATCH_STATS_DTYPE = np.dtype(STATS_DTYPE.descr + [("h0u", "<f8"), ("next_h", "<f8"),
+                                                  ("next_q", "<i8")])
 
 
 def write_bin(batch: KineticsBatch, path) -> None:
