@@ -113,6 +113,24 @@ SUNGB300_EXPORT int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0,
 /* Wall time of the last Solve's integration kernel in milliseconds. */
 SUNGB300_EXPORT double SUNBatchBDF_GB300_LastKernelMs(SUNBatchBDF_GB300 b);
 
+/* Systems that end a fast-mode solve with a failure flag (CVode < 0) are
+ * integrated again, on the device and in the same stream, by a second launch
+ * in the retry mode: SUNBATCHBDF_RETRY_OTHER (default: the other fast mode,
+ * MIXED <-> FP64, about 1% of a solve when a handful of systems fail),
+ * SUNBATCHBDF_FP64_EXACT (the reference's own arithmetic, so those systems'
+ * flags and results are the reference CVODE's; one exact integration is
+ * ~0.3 s on an otherwise idle GPU), SUNBATCHBDF_FP64 or SUNBATCHBDF_MIXED;
+ * SUNBATCHBDF_RETRY_OFF turns it off.  Retried systems report the retry's
+ * yout and stats.  A fast-mode failure is a rounding-sensitive edge case of
+ * CVODE's error-test heuristics (repeated test failures at one step), and the
+ * two fast modes fail on different systems.  No counterpart in the reference
+ * (one CVODE instance per system has no other form to fall back to). */
+#define SUNBATCHBDF_RETRY_OFF   (-1)
+#define SUNBATCHBDF_RETRY_OTHER (-2)
+SUNGB300_EXPORT int SUNBatchBDF_GB300_SetRetryMode(SUNBatchBDF_GB300 b, int mode);
+/* Number of systems the last solve integrated again. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_GetRetryCount(SUNBatchBDF_GB300 b, long long* nretry);
+
 /* Statistics of system `sys` (host array from Solve) in the layout of
  * CVodePrintAllStats (src/cvode/cvode_io.c:1626): the same names, order and
  * number formats, fmt 0 = SUN_OUTPUTFORMAT_TABLE, 1 = SUN_OUTPUTFORMAT_CSV; the

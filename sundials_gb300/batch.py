@@ -35,6 +35,8 @@ def _declare(lib):
         ("SUNBatchBDF_GB300_GetPredictorCounts", ct.c_int,
          [vp, ct.POINTER(ct.c_longlong), ct.POINTER(ct.c_longlong)]),
         ("SUNBatchBDF_GB300_SetRecorder", ct.c_int, [vp, vp, vp, ct.c_longlong, vp]),
+        ("SUNBatchBDF_GB300_SetRetryMode", ct.c_int, [vp, ct.c_int]),
+        ("SUNBatchBDF_GB300_GetRetryCount", ct.c_int, [vp, ct.POINTER(ct.c_longlong)]),
     ]:
         f = getattr(lib, name)
         f.restype = res
@@ -61,8 +63,13 @@ class BatchBDF:
             raise RuntimeError("SUNBatchBDF_GB300_Create failed: "
                                + self.lib.SUNGB300_GetLastErrorMessage().decode())
 
-    def configure(self, rtol=1e-6, atol=1e-12, mode="fp64", mxstep=1000000, refine=1):
+    def configure(self, rtol=1e-6, atol=1e-12, mode="fp64", mxstep=1000000, refine=1,
+                  retry="other"):
+        """retry: mode for systems that fail in a fast mode ("other" fast mode,
+        "fp64_exact", "fp64", "mixed", or None for no retry)."""
         L = self.lib
+        rmode = {None: -1, "other": -2}.get(retry, MODES.get(retry))
+        assert L.SUNBatchBDF_GB300_SetRetryMode(self.h, rmode) == 0
         assert L.SUNBatchBDF_GB300_SetTolerances(self.h, rtol, atol) == 0
         assert L.SUNBatchBDF_GB300_SetMode(self.h, MODES[mode] if isinstance(mode, str) else mode) == 0
         assert L.SUNBatchBDF_GB300_SetMaxNumSteps(self.h, mxstep) == 0
@@ -95,6 +102,12 @@ class BatchBDF:
         if rc != 0:
             raise RuntimeError(f"SUNBatchBDF_GB300_SetPredictor failed ({rc})")
         self._mlp = mlp
+
+    @property
+    def retry_count(self) -> int:
+        n = ct.c_longlong()
+        assert self.lib.SUNBatchBDF_GB300_GetRetryCount(self.h, ct.byref(n)) == 0
+        return n.value
 
     def predictor_counts(self):
         calls, kept = ct.c_longlong(), ct.c_longlong()

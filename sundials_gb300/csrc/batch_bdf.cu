@@ -57,6 +57,10 @@ struct SUNBatchBDF_GB300_
   float* rec_t    = nullptr;
   unsigned long long* rec_count = nullptr;
   long long rec_cap = 0;
+  // retry of failed systems (fast modes): mode of the retry launch, or -1
+  int retry_mode   = -2;  // the other fast mode
+
+  int32_t* d_fail  = nullptr;  // [nsys] ids of failed systems
 };
 
 namespace {
@@ -224,7 +228,9 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
        gb300::check_cuda(cudaMalloc(&b->d_yout, sizeof(double) * b->Y), "cudaMalloc(yout)") &&
        gb300::check_cuda(cudaMalloc(&b->d_stats, sizeof(SUNBatchBDFStats) * nsys),
                          "cudaMalloc(stats)") &&
-       gb300::check_cuda(cudaMalloc(&b->d_next, 2 * sizeof(unsigned int)), "cudaMalloc(next)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_next, 4 * sizeof(unsigned int)), "cudaMalloc(next)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_fail, sizeof(int32_t) * (nsys ? nsys : 1)),
+                         "cudaMalloc(failed list)") &&
        gb300::check_cuda(cudaEventCreate(&b->ev0), "cudaEventCreate") &&
        gb300::check_cuda(cudaEventCreate(&b->ev1), "cudaEventCreate");
   // Scratch for the largest grid any mode launches, so that SolveAsync
@@ -341,7 +347,15 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.rec_t     = b->rec_t;
   P.rec_count = b->rec_count;
   P.rec_cap   = b->rec_cap;
-  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 2 * sizeof(unsigned int), b->stream),
+  // d_next: [0], [1] the buckets' queues, [2] the retry queue, [3] failed count
+  const int rmode  = b->retry_mode == -2
+                      ? (b->mode == SUNBATCHBDF_MIXED ? SUNBATCHBDF_FP64 : SUNBATCHBDF_MIXED)
+                      : b->retry_mode;
+  const bool retry = fast && rmode >= 0;
+  P.fail_list  = retry ? b->d_fail : nullptr;
+  P.fail_count = b->d_next + 3;
+  P.count_dev  = nullptr;
+  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 4 * sizeof(unsigned int), b->stream),
                          "cudaMemsetAsync(queue)"))
     return SUN_ERR_EXT_FAIL;
   if (P.lp_counts &&
@@ -363,8 +377,49 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
                         b->d_next + bucket);
     gb300::count_launch();
   }
+  if (retry && e == cudaSuccess)
+  {
+    // systems that failed in the fast mode are integrated again in the retry
+    // mode (by default the exact mode: the reference's own arithmetic); the
+    // queue length is the device-side failure count, so nothing waits on the host
+    Params R      = P;
+    R.fail_list   = nullptr;
+    R.count_dev   = b->d_next + 3;
+    R.mlp_w       = nullptr;
+    R.mlp_b       = nullptr;
+    R.lp_counts   = nullptr;
+    R.rec_x       = nullptr;
+    const int grid = std::min(gb300::num_sms(), b->slots);
+    e = (rmode == SUNBATCHBDF_FP64_EXACT)
+          ? launch_exact(R, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 2)
+          : launch_fast(R, rmode, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 2);
+    gb300::count_launch();
+  }
   cudaEventRecord(b->ev1, b->stream);
   return gb300::check_cuda(e, "k_batch_bdf launch") ? SUN_SUCCESS : SUN_ERR_EXT_FAIL;
+}
+
+int SUNBatchBDF_GB300_SetRetryMode(SUNBatchBDF_GB300 b, int mode)
+{
+  if (!b) return SUN_ERR_ARG_CORRUPT;
+  if (mode != -1 && mode != -2 && mode != SUNBATCHBDF_FP64_EXACT && mode != SUNBATCHBDF_FP64 &&
+      mode != SUNBATCHBDF_MIXED)
+    return SUN_ERR_ARG_OUTOFRANGE;
+  b->retry_mode = mode;
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_GetRetryCount(SUNBatchBDF_GB300 b, long long* nretry)
+{
+  if (!b || !nretry) return SUN_ERR_ARG_CORRUPT;
+  unsigned int h = 0;
+  if (!gb300::check_cuda(cudaMemcpyAsync(&h, b->d_next + 3, sizeof h, cudaMemcpyDeviceToHost,
+                                         b->stream),
+                         "cudaMemcpyAsync(retry count)") ||
+      !gb300::check_cuda(cudaStreamSynchronize(b->stream), "retry count"))
+    return SUN_ERR_EXT_FAIL;
+  *nretry = (long long)h;
+  return SUN_SUCCESS;
 }
 
 int SUNBatchBDF_GB300_Solve(SUNBatchBDF_GB300 b, double t0, const double* y0, double tout,
@@ -487,6 +542,7 @@ void SUNBatchBDF_GB300_Free(SUNBatchBDF_GB300 b)
   cudaFree(b->d_yout);
   cudaFree(b->d_stats);
   cudaFree(b->d_next);
+  cudaFree(b->d_fail);
   cudaFree(b->d_scratch);
   cudaFree(b->d_piv);
   cudaFree(b->d_timers);

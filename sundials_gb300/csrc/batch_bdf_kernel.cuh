@@ -114,6 +114,12 @@ struct Params
   float* rec_t;            // [cap][64]
   unsigned long long* rec_count;
   long long rec_cap;
+  // retry of failed systems: a fast-mode launch appends the ids of systems
+  // that end with a failure flag to fail_list (fail_count entries); the retry
+  // launch processes order = fail_list with its length read from count_dev
+  int32_t* fail_list;
+  unsigned int* fail_count;
+  const unsigned int* count_dev;
 };
 
 // Per-warp shared-memory slice for systems of at most NB species; the warp's
@@ -1721,6 +1727,8 @@ struct Integrator
       st.next_q  = next_q;
       P.stats[s] = st;
     }
+    if (lane == 0 && P.fail_list && istate != CV_SUCCESS)
+      P.fail_list[atomicAdd(P.fail_count, 1u)] = (int32_t)s;
     if (lane == 0 && P.lp_counts && nlp > 0)
     {
       atomicAdd(P.lp_counts, (unsigned long long)nlp);
@@ -1747,6 +1755,11 @@ __global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
   WarpMem<NB>* mem = (WarpMem<NB>*)smem;
   void* mat        = L::mat_in_smem ? (void*)(smem + L::mem_bytes) : (void*)(scratch + SLOT_J);
   Integrator<MODE, NB> I(P, *mem, mat, lane);
+  if (P.count_dev)
+  {  // a retry launch: its queue length was produced on the device
+    const int64_t c = (int64_t)*P.count_dev;
+    count           = c < count ? c : count;
+  }
   for (;;)
   {
     unsigned int idx = 0;

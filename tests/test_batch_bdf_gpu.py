@@ -33,7 +33,7 @@ from sundials_gb300.batch import BatchBDF
 
 pytestmark = pytest.mark.gpu
 GOLD = Path(__file__).resolve().parent / "golden" / "kinetics_cvode_ref.npz"
-RTOL, ATOL = 1e-6, 1e-12
+RTOL, ATOL, TOUT = 1e-6, 1e-12, 100.0
 
 
 @pytest.fixture(scope="module")
@@ -110,3 +110,37 @@ def test_deterministic_and_order_independent(gb300_lib, sample):
     y3, s3 = BatchBDF(one).configure(RTOL, ATOL, "fp64").solve(100.0)
     assert np.array_equal(y3.view(np.int64), per_system(sample, y1)[7].view(np.int64))
     assert s3["nst"][0] == s1["nst"][7]
+
+
+def test_failed_systems_are_retried_in_the_exact_mode():
+    """Systems of the seed-1 batch that end the fast modes with CV_ERR_FAILURE
+    (seven repeated error-test failures at one step; rounding-sensitive edge
+    cases) while the reference's CVODE integrates them.  The default retry
+    (the other fast mode) leaves exactly the reference's failure set here; the
+    exact-mode retry also gives those systems the reference's results, bit for
+    bit."""
+    from oracle import port
+    ids = np.array([6038, 11303, 13961, 14721, 16706, 20958, 25041, 26550, 32185, 38641,
+                    49477, 53931, 56464, 62223])
+    sub = K.generate(65536, seed=1).subset(ids)
+    pst, pys = port.bdf_batch(sub, dd_pow=True)
+    assert list(np.nonzero(pst["flag"] != 0)[0]) == [10]  # system 49477 fails in the reference
+    y_exact, st_exact = BatchBDF(sub).configure(RTOL, ATOL, "fp64_exact").solve(TOUT)
+    for mode in ("mixed", "fp64"):
+        B0 = BatchBDF(sub).configure(RTOL, ATOL, mode, retry=None)
+        _, st0 = B0.solve(TOUT)
+        assert B0.retry_count == 0
+        failed_fast = np.nonzero(st0["flag"] != 0)[0]
+        assert len(failed_fast) >= 2, mode  # the fast mode alone fails on some of them
+        Bo = BatchBDF(sub).configure(RTOL, ATOL, mode)
+        _, sto = Bo.solve(TOUT)
+        assert Bo.retry_count == len(failed_fast)
+        assert np.array_equal(sto["flag"], pst["flag"])
+        B = BatchBDF(sub).configure(RTOL, ATOL, mode, retry="fp64_exact")
+        y, st = B.solve(TOUT)
+        assert B.retry_count == len(failed_fast)
+        assert np.array_equal(st["flag"], pst["flag"])
+        for k in failed_fast:
+            a, b_ = sub.y_off[k], sub.y_off[k + 1]
+            assert np.array_equal(y[a:b_], y_exact[a:b_])
+            assert st["nst"][k] == st_exact["nst"][k]
