@@ -501,7 +501,8 @@ def run_kinetics(args, world, rank, local):
         "ms_per_step": round(float(np.mean(times)) * 1e3, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (FP32 Newton-matrix inverse)",
         "data": "synthetic (seeded mass-action networks, sundials_gb300/kinetics.py)",
-        "config": {"workload": "uneven stiff kinetics batch (configs[2])", "systems": nsys,
+        "config": {"workload": f"uneven stiff kinetics batch: {nsys:,} mass-action systems, "
+                               "n ~ U{8..64}, 2n reactions", "systems": nsys,
                    "species": "U{8..64}", "reactions_per_system": "2n", "rtol": RTOL,
                    "atol": ATOL, "t": [0.0, TOUT], "method": "BDF q<=5, Newton, dense",
                    "form": f"MIXED (FP32 Gauss-Jordan inverse + {args.refine} FP64 refinement sweep)",
@@ -579,7 +580,8 @@ def run_reference(args, world, rank):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(args.nsys / value * 1e3, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "uneven stiff kinetics batch (configs[2])", "systems": args.nsys,
+        "config": {"workload": f"uneven stiff kinetics batch: {args.nsys:,} mass-action systems, "
+                               "n ~ U{8..64}, 2n reactions", "systems": args.nsys,
                    "rtol": RTOL, "atol": ATOL, "t": [0.0, TOUT]},
         "cpu_baseline": {"value": round(value, 2), "unit": "systems/s", "cores": cb["cores"],
                          "kind": "port", "sample": cb["sample"]},
