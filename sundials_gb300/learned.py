@@ -94,3 +94,22 @@ def pipeline(train_nsys=8192, seeds=4, capacity=1 << 20, epochs=8, mlp_seed=7):
     t2 = time.perf_counter()
     return mlp, {"rows": int(X.shape[0]), "record_s": t1 - t0, "train_s": t2 - t1,
                  "losses": losses, "target_var": float(T.var().item())}
+
+
+def _main(argv=None):
+    """Record and train (a profiling and smoke entry):
+    python -m sundials_gb300.learned --nsys 2048 --seeds 1 --epochs 1"""
+    import argparse
+    import json
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--nsys", type=int, default=2048)
+    ap.add_argument("--seeds", type=int, default=1)
+    ap.add_argument("--epochs", type=int, default=1)
+    ap.add_argument("--capacity", type=int, default=1 << 19)
+    args = ap.parse_args(argv)
+    _, info = pipeline(args.nsys, args.seeds, args.capacity, args.epochs)
+    print(json.dumps(info))
+
+
+if __name__ == "__main__":
+    _main()
