@@ -22,8 +22,9 @@ cudaError_t launch_exact(const Params& P, int nb, int grid, cudaStream_t stream,
 cudaError_t occupancy_exact(int nb, int* per_sm);
 }  // namespace bdf
 
-// Systems are processed in two size buckets, n <= 32 and 32 < n <= 64, each
-// by its own persistent launch whose shared memory is sized for the bucket.
+// Systems are sorted into size classes n <= 32, 32 < n <= 48, 48 < n <= 64;
+// each class (or, in the FP64 modes, n <= 32 and n > 32) is one persistent
+// launch whose shared memory is sized for it (see plan()).
 
 using namespace bdf;
 
@@ -45,10 +46,11 @@ struct SUNBatchBDF_GB300_
   int* d_piv = nullptr;
   long long* d_timers = nullptr;
   int slots = 0;
-  const int32_t* d_order[2] = {nullptr, nullptr};  // [0]: n <= 32, [1]: n > 32
-  int64_t count[2]          = {0, 0};
+  const int32_t* d_order[3] = {nullptr, nullptr, nullptr};  // n <= 32, <= 48, <= 64
+  int64_t count[3]          = {0, 0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   float last_ms = 0.f;
+
   // learned predictor and training-data recorder
   const uint16_t* mlp_w = nullptr;
   const float* mlp_b    = nullptr;
@@ -89,17 +91,46 @@ bool is_device_ptr(const void* p)
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-int grid_for(SUNBatchBDF_GB300 b, int mode, int bucket)
+constexpr int kBuckets = 3;
+
+int grid_for(int mode, int nb, int64_t need)
 {
-  const int nb  = bucket ? 64 : 32;
   int per_sm    = 0;
   cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(nb, &per_sm)
                                                    : occupancy_fast(mode, nb, &per_sm);
   if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-  int grid     = gb300::num_sms() * per_sm;
-  int64_t need = b->count[bucket];
+  int grid = gb300::num_sms() * per_sm;
   if (need < grid) grid = (int)need;
   return grid < 1 ? 1 : grid;
+}
+
+// One persistent launch per size class, largest systems first.  MIXED keeps
+// an n x (n+4) FP32 inverse per warp in shared memory, so a 48-wide class
+// (12 warps/SM) pays for its extra tail; the FP64 modes are register-limited
+// at the same occupancy for every width and run n > 32 as one class.
+struct Launch
+{
+  int nb, grid;
+  const int32_t* order;
+  int64_t count;
+  int queue;
+};
+
+int plan(SUNBatchBDF_GB300 b, int mode, Launch* L)
+{
+  int nl = 0;
+  auto add = [&](int nb, const int32_t* order, int64_t count, int queue) {
+    if (count <= 0) return;
+    L[nl++] = {nb, grid_for(mode, nb, count), order, count, queue};
+  };
+  if (mode == SUNBATCHBDF_MIXED)
+  {
+    add(64, b->d_order[2], b->count[2], 2);
+    add(48, b->d_order[1], b->count[1], 1);
+  }
+  else add(64, b->d_order[2], b->count[2] + b->count[1], 2);
+  add(32, b->d_order[0], b->count[0], 0);
+  return nl;
 }
 
 bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
@@ -198,10 +229,13 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int32_t x, int32_t y) { return prob->n[x] > prob->n[y]; });
-  int64_t nbig = 0;
-  while (nbig < nsys && prob->n[order[nbig]] > 32) nbig++;
-  b->count[1] = nbig;
-  b->count[0] = nsys - nbig;
+  int64_t n64 = 0, n48 = 0;  // order is by decreasing n
+  while (n64 < nsys && prob->n[order[n64]] > 48) n64++;
+  n48 = n64;
+  while (n48 < nsys && prob->n[order[n48]] > 32) n48++;
+  b->count[2] = n64;
+  b->count[1] = n48 - n64;
+  b->count[0] = nsys - n48;
 
   DevProblem& d = b->dp;
   d.nsys   = nsys;
@@ -220,15 +254,16 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   d.jent   = upload(b, jent.data(), jent.size());
   d.je_off = upload(b, je_off.data(), je_off.size());
   d.order  = upload(b, order.data(), order.size());
-  b->d_order[1] = d.order;
-  b->d_order[0] = d.order + nbig;
+  b->d_order[2] = d.order;
+  b->d_order[1] = d.order + n64;
+  b->d_order[0] = d.order + n48;
   bool ok  = d.n && d.y_off && d.r_off && d.rtype && d.ra && d.rb && d.rc && d.rk && d.fptr &&
             d.fent && d.e_off && d.jptr && d.jent && d.je_off && d.order;
   ok = ok && gb300::check_cuda(cudaMalloc(&b->d_y0, sizeof(double) * b->Y), "cudaMalloc(y0)") &&
        gb300::check_cuda(cudaMalloc(&b->d_yout, sizeof(double) * b->Y), "cudaMalloc(yout)") &&
        gb300::check_cuda(cudaMalloc(&b->d_stats, sizeof(SUNBatchBDFStats) * nsys),
                          "cudaMalloc(stats)") &&
-       gb300::check_cuda(cudaMalloc(&b->d_next, 4 * sizeof(unsigned int)), "cudaMalloc(next)") &&
+       gb300::check_cuda(cudaMalloc(&b->d_next, 5 * sizeof(unsigned int)), "cudaMalloc(next)") &&
        gb300::check_cuda(cudaMalloc(&b->d_fail, sizeof(int32_t) * (nsys ? nsys : 1)),
                          "cudaMalloc(failed list)") &&
        gb300::check_cuda(cudaEventCreate(&b->ev0), "cudaEventCreate") &&
@@ -237,7 +272,11 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   // allocates nothing.
   int maxgrid = 1;
   for (int mode : {SUNBATCHBDF_FP64, SUNBATCHBDF_MIXED, SUNBATCHBDF_FP64_EXACT})
-    for (int bucket = 0; bucket < 2; bucket++) maxgrid = std::max(maxgrid, grid_for(b, mode, bucket));
+  {
+    Launch L[kBuckets];
+    const int nl = plan(b, mode, L);
+    for (int k = 0; k < nl; k++) maxgrid = std::max(maxgrid, L[k].grid);
+  }
   ok = ok && ensure_scratch(b, maxgrid);
   if (!ok)
   {
@@ -347,15 +386,15 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.rec_t     = b->rec_t;
   P.rec_count = b->rec_count;
   P.rec_cap   = b->rec_cap;
-  // d_next: [0], [1] the buckets' queues, [2] the retry queue, [3] failed count
+  // d_next: [0..2] the buckets' queues, [3] the retry queue, [4] failed count
   const int rmode  = b->retry_mode == -2
                       ? (b->mode == SUNBATCHBDF_MIXED ? SUNBATCHBDF_FP64 : SUNBATCHBDF_MIXED)
                       : b->retry_mode;
   const bool retry = fast && rmode >= 0;
   P.fail_list  = retry ? b->d_fail : nullptr;
-  P.fail_count = b->d_next + 3;
+  P.fail_count = b->d_next + 4;
   P.count_dev  = nullptr;
-  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 4 * sizeof(unsigned int), b->stream),
+  if (!gb300::check_cuda(cudaMemsetAsync(b->d_next, 0, 5 * sizeof(unsigned int), b->stream),
                          "cudaMemsetAsync(queue)"))
     return SUN_ERR_EXT_FAIL;
   if (P.lp_counts &&
@@ -364,35 +403,34 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
     return SUN_ERR_EXT_FAIL;
   cudaEventRecord(b->ev0, b->stream);
   cudaError_t e = cudaSuccess;
-  for (int bucket = 1; bucket >= 0 && e == cudaSuccess; bucket--)
-  {  // large systems first, then the small-system bucket
-    if (b->count[bucket] == 0) continue;
-    const int grid = grid_for(b, b->mode, bucket);
-    if (grid > b->slots) return SUN_ERR_MEM_FAIL;
-    const int nb = bucket ? 64 : 32;
+  Launch L[kBuckets];
+  const int nl = plan(b, b->mode, L);
+  for (int k = 0; k < nl && e == cudaSuccess; k++)
+  {
+    if (L[k].grid > b->slots) return SUN_ERR_MEM_FAIL;
     e = (b->mode == SUNBATCHBDF_FP64_EXACT)
-          ? launch_exact(P, nb, grid, b->stream, b->d_order[bucket], b->count[bucket],
-                         b->d_next + bucket)
-          : launch_fast(P, b->mode, nb, grid, b->stream, b->d_order[bucket], b->count[bucket],
-                        b->d_next + bucket);
+          ? launch_exact(P, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
+                         b->d_next + L[k].queue)
+          : launch_fast(P, b->mode, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
+                        b->d_next + L[k].queue);
     gb300::count_launch();
   }
   if (retry && e == cudaSuccess)
   {
     // systems that failed in the fast mode are integrated again in the retry
-    // mode (by default the exact mode: the reference's own arithmetic); the
-    // queue length is the device-side failure count, so nothing waits on the host
+    // mode (by default the other fast mode); the queue length is the
+    // device-side failure count, so nothing waits on the host
     Params R      = P;
     R.fail_list   = nullptr;
-    R.count_dev   = b->d_next + 3;
+    R.count_dev   = b->d_next + 4;
     R.mlp_w       = nullptr;
     R.mlp_b       = nullptr;
     R.lp_counts   = nullptr;
     R.rec_x       = nullptr;
     const int grid = std::min(gb300::num_sms(), b->slots);
     e = (rmode == SUNBATCHBDF_FP64_EXACT)
-          ? launch_exact(R, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 2)
-          : launch_fast(R, rmode, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 2);
+          ? launch_exact(R, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 3)
+          : launch_fast(R, rmode, 64, grid, b->stream, b->d_fail, b->nsys, b->d_next + 3);
     gb300::count_launch();
   }
   cudaEventRecord(b->ev1, b->stream);
@@ -413,7 +451,7 @@ int SUNBatchBDF_GB300_GetRetryCount(SUNBatchBDF_GB300 b, long long* nretry)
 {
   if (!b || !nretry) return SUN_ERR_ARG_CORRUPT;
   unsigned int h = 0;
-  if (!gb300::check_cuda(cudaMemcpyAsync(&h, b->d_next + 3, sizeof h, cudaMemcpyDeviceToHost,
+  if (!gb300::check_cuda(cudaMemcpyAsync(&h, b->d_next + 4, sizeof h, cudaMemcpyDeviceToHost,
                                          b->stream),
                          "cudaMemcpyAsync(retry count)") ||
       !gb300::check_cuda(cudaStreamSynchronize(b->stream), "retry count"))

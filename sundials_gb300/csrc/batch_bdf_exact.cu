@@ -30,13 +30,14 @@ static cudaError_t occ_one(int* per_sm)
 cudaError_t launch_exact(const Params& P, int nb, int grid, cudaStream_t stream,
                          const int32_t* order, int64_t count, unsigned int* next)
 {
-  return nb <= 32 ? launch_one<32>(P, grid, stream, order, count, next)
-                  : launch_one<64>(P, grid, stream, order, count, next);
+  return nb <= 32   ? launch_one<32>(P, grid, stream, order, count, next)
+         : nb <= 48 ? launch_one<48>(P, grid, stream, order, count, next)
+                    : launch_one<64>(P, grid, stream, order, count, next);
 }
 
 cudaError_t occupancy_exact(int nb, int* per_sm)
 {
-  return nb <= 32 ? occ_one<32>(per_sm) : occ_one<64>(per_sm);
+  return nb <= 32 ? occ_one<32>(per_sm) : nb <= 48 ? occ_one<48>(per_sm) : occ_one<64>(per_sm);
 }
 
 }  // namespace bdf

@@ -1,5 +1,5 @@
 // batch_bdf_fast.cu -- instantiates the batched BDF kernel for the FP64 (FMA)
-// and MIXED (FP32 inverse + FP64 refinement) modes, both size buckets.
+// and MIXED (FP32 inverse + FP64 refinement) modes, all three size buckets.
 #include "batch_bdf_kernel.cuh"
 
 namespace bdf {
@@ -26,17 +26,23 @@ cudaError_t launch_fast(const Params& P, int mode, int nb, int grid, cudaStream_
                         const int32_t* order, int64_t count, unsigned int* next)
 {
   if (mode == SUNBATCHBDF_MIXED)
-    return nb <= 32 ? launch_one<SUNBATCHBDF_MIXED, 32>(P, grid, stream, order, count, next)
-                    : launch_one<SUNBATCHBDF_MIXED, 64>(P, grid, stream, order, count, next);
-  return nb <= 32 ? launch_one<SUNBATCHBDF_FP64, 32>(P, grid, stream, order, count, next)
-                  : launch_one<SUNBATCHBDF_FP64, 64>(P, grid, stream, order, count, next);
+    return nb <= 32   ? launch_one<SUNBATCHBDF_MIXED, 32>(P, grid, stream, order, count, next)
+           : nb <= 48 ? launch_one<SUNBATCHBDF_MIXED, 48>(P, grid, stream, order, count, next)
+                      : launch_one<SUNBATCHBDF_MIXED, 64>(P, grid, stream, order, count, next);
+  return nb <= 32   ? launch_one<SUNBATCHBDF_FP64, 32>(P, grid, stream, order, count, next)
+         : nb <= 48 ? launch_one<SUNBATCHBDF_FP64, 48>(P, grid, stream, order, count, next)
+                    : launch_one<SUNBATCHBDF_FP64, 64>(P, grid, stream, order, count, next);
 }
 
 cudaError_t occupancy_fast(int mode, int nb, int* per_sm)
 {
   if (mode == SUNBATCHBDF_MIXED)
-    return nb <= 32 ? occ_one<SUNBATCHBDF_MIXED, 32>(per_sm) : occ_one<SUNBATCHBDF_MIXED, 64>(per_sm);
-  return nb <= 32 ? occ_one<SUNBATCHBDF_FP64, 32>(per_sm) : occ_one<SUNBATCHBDF_FP64, 64>(per_sm);
+    return nb <= 32   ? occ_one<SUNBATCHBDF_MIXED, 32>(per_sm)
+           : nb <= 48 ? occ_one<SUNBATCHBDF_MIXED, 48>(per_sm)
+                      : occ_one<SUNBATCHBDF_MIXED, 64>(per_sm);
+  return nb <= 32   ? occ_one<SUNBATCHBDF_FP64, 32>(per_sm)
+         : nb <= 48 ? occ_one<SUNBATCHBDF_FP64, 48>(per_sm)
+                    : occ_one<SUNBATCHBDF_FP64, 64>(per_sm);
 }
 
 }  // namespace bdf
