@@ -61,6 +61,7 @@ struct SUNBatchBDF_GB300_
   long long rec_cap = 0;
   // retry of failed systems (fast modes): mode of the retry launch, or -1
   int retry_mode   = -2;  // the other fast mode
+  int per_sm[3][3] = {};   // [mode][width class] resident warps per SM
 
   int32_t* d_fail  = nullptr;  // [nsys] ids of failed systems
 };
@@ -93,13 +94,29 @@ bool is_device_ptr(const void* p)
 
 constexpr int kBuckets = 3;
 
-int grid_for(int mode, int nb, int64_t need)
+// Resident warps per SM of every (mode, width) instantiation, queried once at
+// creation (the query also sets each kernel's dynamic shared-memory limit), so
+// that SolveAsync makes no such call and can be captured into a CUDA graph.
+inline int width_index(int nb) { return nb <= 32 ? 0 : nb <= 48 ? 1 : 2; }
+
+bool query_occupancy(SUNBatchBDF_GB300 b)
 {
-  int per_sm    = 0;
-  cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(nb, &per_sm)
-                                                   : occupancy_fast(mode, nb, &per_sm);
-  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
-  int grid = gb300::num_sms() * per_sm;
+  const int widths[3] = {32, 48, 64};
+  for (int mode : {SUNBATCHBDF_FP64, SUNBATCHBDF_FP64_EXACT, SUNBATCHBDF_MIXED})
+    for (int k = 0; k < 3; k++)
+    {
+      int per_sm    = 0;
+      cudaError_t e = (mode == SUNBATCHBDF_FP64_EXACT) ? occupancy_exact(widths[k], &per_sm)
+                                                       : occupancy_fast(mode, widths[k], &per_sm);
+      if (!gb300::check_cuda(e, "k_batch_bdf occupancy")) return false;
+      b->per_sm[mode][k] = per_sm < 1 ? 1 : per_sm;
+    }
+  return true;
+}
+
+int grid_for(SUNBatchBDF_GB300 b, int mode, int nb, int64_t need)
+{
+  int grid = gb300::num_sms() * b->per_sm[mode][width_index(nb)];
   if (need < grid) grid = (int)need;
   return grid < 1 ? 1 : grid;
 }
@@ -121,7 +138,7 @@ int plan(SUNBatchBDF_GB300 b, int mode, Launch* L)
   int nl = 0;
   auto add = [&](int nb, const int32_t* order, int64_t count, int queue) {
     if (count <= 0) return;
-    L[nl++] = {nb, grid_for(mode, nb, count), order, count, queue};
+    L[nl++] = {nb, grid_for(b, mode, nb, count), order, count, queue};
   };
   if (mode == SUNBATCHBDF_MIXED)
   {
@@ -270,6 +287,7 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
        gb300::check_cuda(cudaEventCreate(&b->ev1), "cudaEventCreate");
   // Scratch for the largest grid any mode launches, so that SolveAsync
   // allocates nothing.
+  ok = ok && query_occupancy(b);
   int maxgrid = 1;
   for (int mode : {SUNBATCHBDF_FP64, SUNBATCHBDF_MIXED, SUNBATCHBDF_FP64_EXACT})
   {

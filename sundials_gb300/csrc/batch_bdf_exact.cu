@@ -6,13 +6,12 @@
 
 namespace bdf {
 
+// (the kernel's shared-memory limit was set by occ_one at creation)
 template <int NB>
 static cudaError_t launch_one(const Params& P, int grid, cudaStream_t stream, const int32_t* order,
                               int64_t count, unsigned int* next)
 {
   const size_t smem = Layout<SUNBATCHBDF_FP64_EXACT, NB>::warp_bytes;
-  cudaFuncSetAttribute(k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB>,
-                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_batch_bdf<SUNBATCHBDF_FP64_EXACT, NB><<<grid, 32, smem, stream>>>(P, order, count, next);
   return cudaGetLastError();
 }

@@ -4,12 +4,12 @@
 
 namespace bdf {
 
+// (the kernel's shared-memory limit was set by occ_one at creation)
 template <int MODE, int NB>
 static cudaError_t launch_one(const Params& P, int grid, cudaStream_t stream, const int32_t* order,
                               int64_t count, unsigned int* next)
 {
   const size_t smem = Layout<MODE, NB>::warp_bytes;
-  cudaFuncSetAttribute(k_batch_bdf<MODE, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   k_batch_bdf<MODE, NB><<<grid, 32, smem, stream>>>(P, order, count, next);
   return cudaGetLastError();
 }

@@ -144,3 +144,32 @@ def test_failed_systems_are_retried_in_the_exact_mode():
             a, b_ = sub.y_off[k], sub.y_off[k + 1]
             assert np.array_equal(y[a:b_], y_exact[a:b_])
             assert st["nst"][k] == st_exact["nst"][k]
+
+
+def test_solve_async_captures_into_a_cuda_graph():
+    """SolveAsync enqueues only stream-ordered work (memsets, the launches of
+    the size classes and the retry launch; queue lengths live on the device),
+    so a whole batch solve captures into a CUDA graph and replays with the
+    direct call's results, bit for bit."""
+    torch = pytest.importorskip("torch")
+    sub = K.generate(4096, seed=1).subset(np.arange(0, 4096, 4))
+    s = torch.cuda.Stream()
+    B = BatchBDF(sub, stream=s.cuda_stream).configure(RTOL, ATOL, "mixed")
+    d_y0 = torch.from_numpy(sub.y0.copy()).cuda()
+    d_y = torch.zeros_like(d_y0)
+    nbytes = K.BATCH_STATS_DTYPE.itemsize * sub.nsys
+    d_st = torch.zeros(nbytes, dtype=torch.uint8, device="cuda")
+    with torch.cuda.stream(s):
+        B.solve_device(d_y0.data_ptr(), d_y.data_ptr(), d_st.data_ptr(), TOUT)
+    s.synchronize()
+    y_direct, st_direct = d_y.cpu().numpy().copy(), d_st.cpu().numpy().copy()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        B.solve_device(d_y0.data_ptr(), d_y.data_ptr(), d_st.data_ptr(), TOUT)
+    for _ in range(2):
+        d_y.zero_()
+        d_st.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(d_y.cpu().numpy(), y_direct)
+        assert np.array_equal(d_st.cpu().numpy(), st_direct)
