@@ -452,8 +452,10 @@ def run_kinetics(args, world, rank, local):
     d_stats = torch.zeros(stats_bytes, dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
-    # ---- headline: MIXED form
+    # ---- headline: MIXED form (launch plan picked by the autotuner on every
+    # 2nd system; the plain form below is tuned the same way)
     B = BatchBDF(batch).configure(RTOL, ATOL, "mixed", refine=args.refine)
+    tune_mixed = B.autotune(stride=2)
     barrier(world)
     clocks = ClockSampler()
     if rank == 0:
@@ -484,6 +486,7 @@ def run_kinetics(args, world, rank, local):
 
     # ---- plain FP64 GPU form of the same solver
     B64 = BatchBDF(batch).configure(RTOL, ATOL, "fp64")
+    tune_fp64 = B64.autotune(stride=2)
     t64 = time_batch(B64, d_y0, d_yout, d_stats, max(1, args.steps // 2), 1, flush)
     plain = nsys * world / max_over_ranks(world, float(np.mean(t64)))
     yout_plain = d_yout.cpu().numpy()
@@ -509,7 +512,11 @@ def run_kinetics(args, world, rank, local):
                    "l2": "512 MB buffer written between timed steps (flush)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single"},
         "plain_fp64_gpu": {"value": round(plain, 1), "unit": "systems/s",
-                           "ms_per_step": round(float(np.mean(t64)) * 1e3, 2)},
+                           "ms_per_step": round(float(np.mean(t64)) * 1e3, 2),
+                           "launch_plan": B64.launch_plan(),
+                           "autotune_ms": {k: round(v, 2) for k, v in tune_fp64.items()}},
+        "launch_plan": B.launch_plan(),
+        "autotune_ms": {k: round(v, 2) for k, v in tune_mixed.items()},
         "speedup_vs_plain_fp64_gpu": round(value / plain, 3),
         "counters_mean": {f: round(float(st[f].mean()), 2) for f in
                           ("nst", "nfe", "nni", "nsetups", "nje", "netf", "ncfn")},

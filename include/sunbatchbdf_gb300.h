@@ -131,6 +131,23 @@ SUNGB300_EXPORT int SUNBatchBDF_GB300_SetRetryMode(SUNBatchBDF_GB300 b, int mode
 /* Number of systems the last solve integrated again. */
 SUNGB300_EXPORT int SUNBatchBDF_GB300_GetRetryCount(SUNBatchBDF_GB300 b, long long* nretry);
 
+/* Launch-plan autotuner (no counterpart in the reference).  A plan is the
+ * set of kernel widths the systems are split into (one persistent launch per
+ * width: systems with n in (previous width, width]): {32,64}, {32,48,64},
+ * {48,64} or {64}.  Autotune integrates every stride-th system of each class
+ * (t0 -> tout, y0 on the host or the device) under every plan, times it
+ * (after a warm-up run when the sample has at most 8,192 systems) and keeps the
+ * fastest plan for the current mode; plan_ms (optional, 4 entries) receives
+ * the times.  The end of each launch is a tail in which few warps still run,
+ * so a sample represents the full batch only if each warp still integrates
+ * many systems: use a small stride (2 for 65,536 systems).  Defaults without
+ * tuning: MIXED {32,48,64}, FP64 modes {32,64}. */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_Autotune(SUNBatchBDF_GB300 b, double t0,
+                                               const double* y0, double tout, int stride,
+                                               double* plan_ms);
+/* The widths of the plan used for `mode` (3 entries, unused ones 0). */
+SUNGB300_EXPORT int SUNBatchBDF_GB300_GetLaunchPlan(SUNBatchBDF_GB300 b, int mode, int* widths);
+
 /* Statistics of system `sys` (host array from Solve) in the layout of
  * CVodePrintAllStats (src/cvode/cvode_io.c:1626): the same names, order and
  * number formats, fmt 0 = SUN_OUTPUTFORMAT_TABLE, 1 = SUN_OUTPUTFORMAT_CSV; the

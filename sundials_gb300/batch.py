@@ -36,6 +36,8 @@ def _declare(lib):
          [vp, ct.POINTER(ct.c_longlong), ct.POINTER(ct.c_longlong)]),
         ("SUNBatchBDF_GB300_SetRecorder", ct.c_int, [vp, vp, vp, ct.c_longlong, vp]),
         ("SUNBatchBDF_GB300_SetRetryMode", ct.c_int, [vp, ct.c_int]),
+        ("SUNBatchBDF_GB300_Autotune", ct.c_int, [vp, ct.c_double, vp, ct.c_double, ct.c_int, vp]),
+        ("SUNBatchBDF_GB300_GetLaunchPlan", ct.c_int, [vp, ct.c_int, vp]),
         ("SUNBatchBDF_GB300_GetRetryCount", ct.c_int, [vp, ct.POINTER(ct.c_longlong)]),
     ]:
         f = getattr(lib, name)
@@ -69,6 +71,7 @@ class BatchBDF:
         "fp64_exact", "fp64", "mixed", or None for no retry)."""
         L = self.lib
         rmode = {None: -1, "other": -2}.get(retry, MODES.get(retry))
+        self._mode = MODES[mode] if isinstance(mode, str) else mode
         assert L.SUNBatchBDF_GB300_SetRetryMode(self.h, rmode) == 0
         assert L.SUNBatchBDF_GB300_SetTolerances(self.h, rtol, atol) == 0
         assert L.SUNBatchBDF_GB300_SetMode(self.h, MODES[mode] if isinstance(mode, str) else mode) == 0
@@ -102,6 +105,24 @@ class BatchBDF:
         if rc != 0:
             raise RuntimeError(f"SUNBatchBDF_GB300_SetPredictor failed ({rc})")
         self._mlp = mlp
+
+    def autotune(self, stride=16, tout=100.0, t0=0.0, y0=None):
+        """Time every launch plan on every stride-th system and keep the
+        fastest for the configured mode; returns {plan widths: ms}."""
+        y0 = np.ascontiguousarray(self.batch.y0 if y0 is None else y0, np.float64)
+        ms = np.zeros(4)
+        rc = self.lib.SUNBatchBDF_GB300_Autotune(self.h, t0, y0.ctypes.data, tout, int(stride),
+                                                 ms.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"SUNBatchBDF_GB300_Autotune failed ({rc})")
+        plans = ["32,64", "32,48,64", "48,64", "64"]
+        return dict(zip(plans, ms.tolist()))
+
+    def launch_plan(self, mode=None):
+        w = np.zeros(3, np.int32)
+        m = MODES[mode] if isinstance(mode, str) else (self._mode if mode is None else mode)
+        assert self.lib.SUNBatchBDF_GB300_GetLaunchPlan(self.h, m, w.ctypes.data) == 0
+        return [int(x) for x in w if x]
 
     @property
     def retry_count(self) -> int:

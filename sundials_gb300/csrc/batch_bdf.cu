@@ -62,6 +62,8 @@ struct SUNBatchBDF_GB300_
   // retry of failed systems (fast modes): mode of the retry launch, or -1
   int retry_mode   = -2;  // the other fast mode
   int per_sm[3][3] = {};   // [mode][width class] resident warps per SM
+  int plan_id[3]   = {0, 0, 1};  // launch plan per mode (index into kPlanWidths)
+  std::vector<int32_t> h_order;   // systems by decreasing n (host copy, for sampling)
 
   int32_t* d_fail  = nullptr;  // [nsys] ids of failed systems
 };
@@ -121,10 +123,13 @@ int grid_for(SUNBatchBDF_GB300 b, int mode, int nb, int64_t need)
   return grid < 1 ? 1 : grid;
 }
 
-// One persistent launch per size class, largest systems first.  MIXED keeps
-// an n x (n+4) FP32 inverse per warp in shared memory, so a 48-wide class
-// (12 warps/SM) pays for its extra tail; the FP64 modes are register-limited
-// at the same occupancy for every width and run n > 32 as one class.
+// One persistent launch per size class, largest systems first.  A launch plan
+// is a set of class widths (the last 64): class k takes the systems with
+// n in (W[k-1], W[k]].  MIXED keeps an n x (n+4) FP32 inverse per warp in
+// shared memory, so a 48-wide class (12 instead of 8 warps/SM) pays for its
+// extra tail; the FP64 modes are register-limited at the same occupancy for
+// every width.  Defaults: MIXED {32, 48, 64}, FP64 modes {32, 64};
+// SUNBatchBDF_GB300_Autotune times every plan on a sample of the batch.
 struct Launch
 {
   int nb, grid;
@@ -133,21 +138,37 @@ struct Launch
   int queue;
 };
 
+constexpr int kPlans = 4;
+const int kPlanWidths[kPlans][3] = {{32, 64, 0}, {32, 48, 64}, {48, 64, 0}, {64, 0, 0}};
+
+// number of systems with n > w (the order is by decreasing n)
+int64_t count_above(SUNBatchBDF_GB300 b, int w)
+{
+  if (w >= 64) return 0;
+  if (w >= 48) return b->count[2];
+  if (w >= 32) return b->count[2] + b->count[1];
+  return b->nsys;
+}
+
+int plan_with(SUNBatchBDF_GB300 b, int mode, int plan_id, const int32_t* order_base, Launch* L)
+{
+  const int* W = kPlanWidths[plan_id];
+  int nw = 0;
+  while (nw < 3 && W[nw]) nw++;
+  int nl = 0;
+  for (int k = nw - 1; k >= 0; k--)
+  {  // largest class first
+    const int64_t hi = count_above(b, k ? W[k - 1] : 0);  // end (exclusive) in the order
+    const int64_t lo = count_above(b, W[k]);
+    if (hi - lo <= 0) continue;
+    L[nl++] = {W[k], grid_for(b, mode, W[k], hi - lo), order_base + lo, hi - lo, k};
+  }
+  return nl;
+}
+
 int plan(SUNBatchBDF_GB300 b, int mode, Launch* L)
 {
-  int nl = 0;
-  auto add = [&](int nb, const int32_t* order, int64_t count, int queue) {
-    if (count <= 0) return;
-    L[nl++] = {nb, grid_for(b, mode, nb, count), order, count, queue};
-  };
-  if (mode == SUNBATCHBDF_MIXED)
-  {
-    add(64, b->d_order[2], b->count[2], 2);
-    add(48, b->d_order[1], b->count[1], 1);
-  }
-  else add(64, b->d_order[2], b->count[2] + b->count[1], 2);
-  add(32, b->d_order[0], b->count[0], 0);
-  return nl;
+  return plan_with(b, mode, b->plan_id[mode], b->d_order[2], L);
 }
 
 bool ensure_scratch(SUNBatchBDF_GB300 b, int slots)
@@ -253,6 +274,7 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   b->count[2] = n64;
   b->count[1] = n48 - n64;
   b->count[0] = nsys - n48;
+  b->h_order  = order;
 
   DevProblem& d = b->dp;
   d.nsys   = nsys;
@@ -291,9 +313,12 @@ SUNBatchBDF_GB300 SUNBatchBDF_GB300_Create(const SUNBatchBDFProblem* prob, void*
   int maxgrid = 1;
   for (int mode : {SUNBATCHBDF_FP64, SUNBATCHBDF_MIXED, SUNBATCHBDF_FP64_EXACT})
   {
-    Launch L[kBuckets];
-    const int nl = plan(b, mode, L);
-    for (int k = 0; k < nl; k++) maxgrid = std::max(maxgrid, L[k].grid);
+    for (int id = 0; id < kPlans; id++)
+    {
+      Launch L[kBuckets];
+      const int nl = plan_with(b, mode, id, b->d_order[2], L);
+      for (int k = 0; k < nl; k++) maxgrid = std::max(maxgrid, L[k].grid);
+    }
   }
   ok = ok && ensure_scratch(b, maxgrid);
   if (!ok)
@@ -377,11 +402,14 @@ int SUNBatchBDF_GB300_GetPredictorCounts(SUNBatchBDF_GB300 b, long long* calls, 
   return SUN_SUCCESS;
 }
 
-int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
-                                 double* d_yout, SUNBatchBDFStats* d_stats)
+namespace {
+// The launch parameters shared by a solve and by the autotuner's trial runs
+// (no predictor, recorder or retry list: the callers add those).
+Params base_params(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
+                   double* d_yout, SUNBatchBDFStats* d_stats)
 {
-  if (!b || !d_y0 || !d_yout) return SUN_ERR_ARG_CORRUPT;
   Params P;
+  memset(&P, 0, sizeof P);
   P.p       = b->dp;
   P.t0      = t0;
   P.tout    = tout;
@@ -396,6 +424,110 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
   P.scratch = b->d_scratch;
   P.pivots  = b->d_piv;
   P.timers  = b->d_timers;
+  return P;
+}
+
+cudaError_t launch_plan(SUNBatchBDF_GB300 b, const Params& P, const Launch* L, int nl)
+{
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nl && e == cudaSuccess; k++)
+  {
+    if (L[k].grid > b->slots) return cudaErrorInvalidConfiguration;
+    e = (b->mode == SUNBATCHBDF_FP64_EXACT)
+          ? launch_exact(P, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
+                         b->d_next + L[k].queue)
+          : launch_fast(P, b->mode, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
+                        b->d_next + L[k].queue);
+    gb300::count_launch();
+  }
+  return e;
+}
+}  // namespace
+
+int SUNBatchBDF_GB300_Autotune(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
+                               int stride, double* plan_ms)
+{
+  if (!b || !d_y0 || stride < 1) return SUN_ERR_ARG_CORRUPT;
+  const int64_t nsys = b->nsys;
+  if (!is_device_ptr(d_y0))
+  {  // a host array: tune on the library's own device copy
+    if (!gb300::check_cuda(cudaMemcpyAsync(b->d_y0, d_y0, sizeof(double) * b->Y,
+                                           cudaMemcpyHostToDevice, b->stream),
+                           "cudaMemcpyAsync(y0)"))
+      return SUN_ERR_EXT_FAIL;
+    d_y0 = b->d_y0;
+  }
+  int32_t* d_sample  = nullptr;
+  if (!gb300::check_cuda(cudaMalloc(&d_sample, sizeof(int32_t) * (nsys ? nsys : 1)),
+                         "cudaMalloc(autotune sample)"))
+    return SUN_ERR_MEM_FAIL;
+  Params P  = base_params(b, t0, d_y0, tout, b->d_yout, b->d_stats);
+  int best  = b->plan_id[b->mode];
+  float bms = 0.f;
+  int rc    = SUN_SUCCESS;
+  for (int id = 0; id < kPlans && rc == SUN_SUCCESS; id++)
+  {
+    // the plan's classes, each reduced to every stride-th system (in the
+    // classes' own largest-first order)
+    Launch full[kBuckets], L[kBuckets];
+    const int nl = plan_with(b, b->mode, id, b->d_order[2], full);
+    std::vector<int32_t> h;
+    int nls = 0;
+    for (int k = 0; k < nl; k++)
+    {
+      const int64_t lo = full[k].order - b->d_order[2], start = (int64_t)h.size();
+      for (int64_t j = lo; j < lo + full[k].count; j += stride) h.push_back(b->h_order[j]);
+      const int64_t cnt = (int64_t)h.size() - start;
+      L[nls++] = {full[k].nb, grid_for(b, b->mode, full[k].nb, cnt), d_sample + start, cnt,
+                  full[k].queue};
+    }
+    if (!gb300::check_cuda(cudaMemcpyAsync(d_sample, h.data(), sizeof(int32_t) * h.size(),
+                                           cudaMemcpyHostToDevice, b->stream),
+                           "cudaMemcpyAsync(autotune sample)"))
+    {
+      rc = SUN_ERR_EXT_FAIL;
+      break;
+    }
+    float ms = 0.f;
+    const int reps = h.size() > 8192 ? 1 : 2;  // small samples: a warm-up run first
+    for (int rep = 0; rep < reps; rep++)
+    {  // the last run is timed
+      cudaMemsetAsync(b->d_next, 0, 5 * sizeof(unsigned int), b->stream);
+      cudaEventRecord(b->ev0, b->stream);
+      cudaError_t e = launch_plan(b, P, L, nls);
+      cudaEventRecord(b->ev1, b->stream);
+      if (!gb300::check_cuda(e, "autotune launch") ||
+          !gb300::check_cuda(cudaStreamSynchronize(b->stream), "autotune run"))
+      {
+        rc = SUN_ERR_EXT_FAIL;
+        break;
+      }
+      cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+    }
+    if (plan_ms) plan_ms[id] = ms;
+    if (rc == SUN_SUCCESS && (id == 0 || ms < bms))
+    {
+      bms  = ms;
+      best = id;
+    }
+  }
+  cudaFree(d_sample);
+  if (rc == SUN_SUCCESS) b->plan_id[b->mode] = best;
+  return rc;
+}
+
+int SUNBatchBDF_GB300_GetLaunchPlan(SUNBatchBDF_GB300 b, int mode, int* widths)
+{
+  if (!b || !widths || mode < 0 || mode > 2) return SUN_ERR_ARG_CORRUPT;
+  for (int k = 0; k < 3; k++) widths[k] = kPlanWidths[b->plan_id[mode]][k];
+  return SUN_SUCCESS;
+}
+
+int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d_y0, double tout,
+                                 double* d_yout, SUNBatchBDFStats* d_stats)
+{
+  if (!b || !d_y0 || !d_yout) return SUN_ERR_ARG_CORRUPT;
+  Params P = base_params(b, t0, d_y0, tout, d_yout, d_stats);
   const bool fast = b->mode != SUNBATCHBDF_FP64_EXACT;  // the exact mode never uses them
   P.mlp_w     = fast ? b->mlp_w : nullptr;
   P.mlp_b     = fast ? b->mlp_b : nullptr;
@@ -420,19 +552,9 @@ int SUNBatchBDF_GB300_SolveAsync(SUNBatchBDF_GB300 b, double t0, const double* d
                          "cudaMemsetAsync(predictor counters)"))
     return SUN_ERR_EXT_FAIL;
   cudaEventRecord(b->ev0, b->stream);
-  cudaError_t e = cudaSuccess;
   Launch L[kBuckets];
-  const int nl = plan(b, b->mode, L);
-  for (int k = 0; k < nl && e == cudaSuccess; k++)
-  {
-    if (L[k].grid > b->slots) return SUN_ERR_MEM_FAIL;
-    e = (b->mode == SUNBATCHBDF_FP64_EXACT)
-          ? launch_exact(P, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
-                         b->d_next + L[k].queue)
-          : launch_fast(P, b->mode, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
-                        b->d_next + L[k].queue);
-    gb300::count_launch();
-  }
+  const int nl  = plan(b, b->mode, L);
+  cudaError_t e = launch_plan(b, P, L, nl);
   if (retry && e == cudaSuccess)
   {
     // systems that failed in the fast mode are integrated again in the retry

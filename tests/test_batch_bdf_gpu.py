@@ -173,3 +173,20 @@ def test_solve_async_captures_into_a_cuda_graph():
         torch.cuda.synchronize()
         assert np.array_equal(d_y.cpu().numpy(), y_direct)
         assert np.array_equal(d_st.cpu().numpy(), st_direct)
+
+
+@pytest.mark.parametrize("mode", ["mixed", "fp64"])
+def test_autotuner_picks_the_fastest_plan_and_plans_agree(mode):
+    """Every launch plan integrates each system with the same arithmetic (the
+    kernel width only sizes the warp's shared memory), so all plans give the
+    same bits; the autotuner keeps the plan it timed fastest."""
+    sub = K.generate(8192, seed=1).subset(np.arange(0, 8192, 4))
+    B = BatchBDF(sub).configure(RTOL, ATOL, mode)
+    y_default, st_default = B.solve(TOUT)
+    times = B.autotune(stride=4)
+    assert all(t > 0 for t in times.values())
+    best = min(times, key=times.get)
+    assert B.launch_plan() == [int(w) for w in best.split(",")]
+    y, st = B.solve(TOUT)
+    assert np.array_equal(y, y_default)
+    assert np.array_equal(st["nst"], st_default["nst"])
