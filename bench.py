@@ -615,7 +615,15 @@ def main():
     ap.add_argument("--spgmr-only", action="store_true",
                     help="print only the SPGMR heat-2D measurement (no kinetics line)")
     ap.add_argument("--spgmr-solves", type=int, default=20)
+    ap.add_argument("--nvector-only", action="store_true",
+                    help="print only the N_Vector microbenchmark (no kinetics line)")
     args = ap.parse_args()
+    if args.nvector_only:
+        import torch
+        torch.cuda.init()
+        print(json.dumps(nvector_measure(args, 0, 0, steps=max(args.steps, 5), warmup=args.warmup)),
+              flush=True)
+        return
     if args.spgmr_only:
         print(json.dumps(spgmr_measure(solves=args.spgmr_solves, warmup=args.warmup)), flush=True)
         return

@@ -502,17 +502,19 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t npair = n >> 1;
     for (int64_t p = tid; p < npair; p += stride)
     {
+      // term 0 starts the sum or is added to z; with NV fixed every later
+      // term's load is issued up front (the loop unrolls completely)
+      const double2 v0 = ((const double2*)args.x[0])[p];
       double2 acc;
-      int k0 = 0;
-      if (accumulate) acc = ((const double2*)z)[p];
-      else
+      if (accumulate)
       {
-        double2 v = ((const double2*)args.x[0])[p];
-        acc       = make_double2(mul(args.c[0], v.x), mul(args.c[0], v.y));
-        k0        = 1;
+        acc   = ((const double2*)z)[p];
+        acc.x = madd<F>(args.c[0], v0.x, acc.x);
+        acc.y = madd<F>(args.c[0], v0.y, acc.y);
       }
+      else acc = make_double2(mul(args.c[0], v0.x), mul(args.c[0], v0.y));
 #pragma unroll 8
-      for (int k = k0; k < nv; ++k)
+      for (int k = 1; k < nv; ++k)
       {
         double2 v = ((const double2*)args.x[k])[p];
         acc.x     = madd<F>(args.c[k], v.x, acc.x);
@@ -984,9 +986,28 @@ bool lincomb_core(N_Vector ref, int nvec, const double* c, N_Vector* X, N_Vector
     }
     int64_t items = vec ? (n + 1) / 2 : n;
     int grid      = stream_grid(items);
-    DISPATCH_F(ref,
-               (k_lincomb<true, 0><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), accumulate, vec)),
-               (k_lincomb<false, 0><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), accumulate, vec)));
+    const int acc_i = accumulate ? 1 : 0;
+    switch (m)
+    {  // fixed term counts unroll completely; longer lists use the run-time loop
+#define LC_CASE(M)                                                                              \
+  case M:                                                                                       \
+    DISPATCH_F(ref, (k_lincomb<true, M><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), acc_i, vec)), \
+               (k_lincomb<false, M><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), acc_i, vec))); \
+    break;
+      LC_CASE(1)
+      LC_CASE(2)
+      LC_CASE(3)
+      LC_CASE(4)
+      LC_CASE(5)
+      LC_CASE(6)
+      LC_CASE(7)
+      LC_CASE(8)
+#undef LC_CASE
+    default:
+      DISPATCH_F(ref,
+                 (k_lincomb<true, 0><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), acc_i, vec)),
+                 (k_lincomb<false, 0><<<grid, kBlock, 0, S(ref)>>>(n, m, args, D(z), acc_i, vec)));
+    }
     count_launch();
     if (!ok_or_report(ref, cudaGetLastError(), "k_lincomb launch")) return false;
     accumulate = true;
