@@ -39,7 +39,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "ODE systems solved/s vs plain FP64 GPU form at rtol 1e-6; N_Vector HBM GB/s"
-NV_BYTES = {"LinearSum": 24, "LinearCombination5": 48, "DotProdMulti5": 48, "WrmsNorm": 16}
+NV_BYTES = {"LinearSum": 24, "LinearCombination5": 48, "DotProdMulti5": 48, "WrmsNorm": 16,
+            "ScaleAddMulti5": 88}
 
 
 def peaks():
@@ -143,42 +144,6 @@ def gen_inputs(n, seed=1):
     return xs, y, w, c5
 
 
-def nvector_cpu_sample(n, threads_all: bool, target_s=10.0):
-    """Time the step's four operations with the oracle's CPU code."""
-    from oracle import port
-    L = port.omp()
-    xs, y, w, c5 = gen_inputs(n, seed=1)
-    z = np.empty(n)
-    z2 = np.empty(n)
-    P = port.ptr
-    d = (ct.c_double * 5)()
-    if not threads_all:
-        os.environ["OMP_NUM_THREADS"] = "1"
-
-    def step():
-        if threads_all:
-            L.omp_linearsum(0.3, P(xs[0]), 0.7, P(y), P(z), n)
-            L.omp_linearcombination(5, P(c5), port.ptrs(xs[:5]), P(z2), n)
-            L.omp_dotprodmulti(5, P(xs[5]), port.ptrs(xs[:5]), d, n)
-            L.omp_wrmsnorm(P(xs[0]), P(w), n)
-        else:
-            L.port_linearsum(0.3, P(xs[0]), 0.7, P(y), P(z), n)
-            L.port_linearcombination(5, P(c5), port.ptrs(xs[:5]), P(z2), n)
-            L.port_dotprodmulti(5, P(xs[5]), port.ptrs(xs[:5]), d, n)
-            L.port_wrmsnorm(P(xs[0]), P(w), n)
-
-    step()
-    reps, t0 = 0, time.perf_counter()
-    while True:
-        step()
-        reps += 1
-        el = time.perf_counter() - t0
-        if el >= target_s or reps >= 1000:
-            break
-    bytes_step = sum(NV_BYTES.values()) * n
-    return bytes_step * reps / el / 1e9, reps, el, (L.omp_threads() if threads_all else 1)
-
-
 def nvector_measure(args, rank, local, steps, warmup):
     """N_Vector microbenchmark on this GPU; returns a dict (per-op GB/s, the
     roofline of the dominant kernel, launch count)."""
@@ -203,8 +168,11 @@ def nvector_measure(args, rank, local, steps, warmup):
     dots = (ct.c_double * 5)()
     evs = {k: [] for k in NV_BYTES}
 
+    a5 = _lib.real_array(c5[::-1].copy() * 1e-3)
+    arrY = _lib.nv_array([v.v for v in X[1:6]])  # Y_k += a_k x in place, as CVODE calls it
+
     def step(timed):
-        e = [torch.cuda.Event(enable_timing=True) for _ in range(5)] if timed else None
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(6)] if timed else None
         if timed:
             e[0].record(stream)
         ops["nvlinearsum"](0.3, X[0].v, 0.7, Y.v, Z.v)
@@ -219,6 +187,9 @@ def nvector_measure(args, rank, local, steps, warmup):
         ops["nvwrmsnorm"](X[0].v, W.v)
         if timed:
             e[4].record(stream)
+        ops["nvscaleaddmulti"](5, a5, X[0].v, arrY, arrY)
+        if timed:
+            e[5].record(stream)
             for k, name in enumerate(NV_BYTES):
                 evs[name].append((e[k], e[k + 1]))
 

@@ -546,7 +546,10 @@ struct SAMArgs
   double* z[kMaxList];
   double a[kMaxList];
 };
-template <bool F>
+// NV > 0: a fixed vector count; every Y_k element pair is loaded before any
+// Z_k is stored (Z_k may be Y_k: in place), so the loads are all in flight at
+// once.  NV == 0: run-time count, one vector at a time.
+template <bool F, int NV>
 __global__ void __launch_bounds__(kBlock)
   k_scaleaddmulti(int64_t n, int nv, const double* x, SAMArgs args, int vec)
 {
@@ -559,6 +562,21 @@ __global__ void __launch_bounds__(kBlock)
     for (int64_t p = tid; p < npair; p += stride)
     {
       double2 xv = ((const double2*)x)[p];
+      if (NV > 0)
+      {
+        double2 yv[NV > 0 ? NV : 1];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) yv[k] = ((const double2*)args.y[k])[p];
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+        {
+          double2 r;
+          r.x                      = madd<F>(args.a[k], xv.x, yv[k].x);
+          r.y                      = madd<F>(args.a[k], xv.y, yv[k].y);
+          ((double2*)args.z[k])[p] = r;
+        }
+        continue;
+      }
 #pragma unroll 6
       for (int k = 0; k < nv; ++k)
       {
@@ -1428,8 +1446,24 @@ SUNErrCode N_VScaleAddMulti_GB300(int nvec, sunrealtype* a, N_Vector x, N_Vector
     }
     int64_t items = vec ? (n + 1) / 2 : n;
     int grid      = stream_grid(items);
-    DISPATCH_F(x, (k_scaleaddmulti<true><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec)),
-               (k_scaleaddmulti<false><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec)));
+    switch (m)
+    {  // fixed vector counts keep every load in flight; longer lists loop
+#define SAM_CASE(M)                                                                           \
+  case M:                                                                                     \
+    DISPATCH_F(x, (k_scaleaddmulti<true, M><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec)), \
+               (k_scaleaddmulti<false, M><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec))); \
+    break;
+      SAM_CASE(1)
+      SAM_CASE(2)
+      SAM_CASE(3)
+      SAM_CASE(4)
+      SAM_CASE(5)
+      SAM_CASE(6)
+#undef SAM_CASE
+    default:
+      DISPATCH_F(x, (k_scaleaddmulti<true, 0><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec)),
+                 (k_scaleaddmulti<false, 0><<<grid, kBlock, 0, S(x)>>>(n, m, D(x), args, vec)));
+    }
     count_launch();
     if (!check_cuda(cudaGetLastError(), "k_scaleaddmulti launch")) return SUN_ERR_EXT_FAIL;
   }
