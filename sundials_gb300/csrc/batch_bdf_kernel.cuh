@@ -140,7 +140,9 @@ struct WarpMem
 // MIXED keeps its FP32 inverse in shared memory (its solves and the FP32
 // elimination are latency-bound); the FP64 modes are bound by the FP64 pipe
 // and run faster with more resident warps, so their LU factors stay in the
-// warp's global scratch (L1/L2-resident).
+// warp's global scratch (L1/L2-resident).  min_blocks caps registers at 128
+// (16 resident one-warp blocks per SM) wherever shared memory allows that
+// many; the 48- and 64-wide MIXED classes are held to 8 by their FP32 inverse.
 template <int MODE, int NB>
 struct Layout
 {
@@ -149,7 +151,7 @@ struct Layout
   static constexpr size_t mem_bytes  = (sizeof(WarpMem<NB>) + 15) / 16 * 16;
   static constexpr size_t mat_bytes  = mat_in_smem ? sizeof(MT) * NB * (NB + 4) : 0;
   static constexpr size_t warp_bytes = mem_bytes + mat_bytes;
-  static constexpr int min_blocks    = mat_in_smem ? 8 : 12;
+  static constexpr int min_blocks    = (mat_in_smem && NB > 32) ? 8 : 16;
 };
 
 // ---------------------------------------------------------------- helpers
