@@ -378,12 +378,9 @@ struct Integrator
     }
     __syncwarp();
     if (MIXED)
-    {  // row-major FP32 copy the Newton matrices are built from until the next J
-      for (int e = lane; e < n * n; e += 32)
-      {
-        const int j = e / n, i = e - j * n;
-        J32[i * n + j] = (float)J[e];
-      }
+    {  // FP32 copy (column-major, like J) the Newton matrices are built from
+       // until the next J
+      for (int e = lane; e < n * n; e += 32) J32[e] = (float)J[e];
       __syncwarp();
     }
     BDF_TOC(t0, T_JAC);
@@ -761,12 +758,24 @@ struct Integrator
     const double c = -gamma;
     int lu;
     if (MIXED)
-    {  // M = I - gamma J in FP32 (row-major, zero padding columns), then its inverse
+    {  // M = I - gamma J in FP32 (row-major, zero padding columns), then its
+       // inverse; four columns of J32 per trip (coalesced loads), stored as
+       // one 16-byte piece of each row (conflict-free: lr = 4 mod 8)
       const float cf = (float)c;
-      for (int e = lane; e < n * lr; e += 32)
+      for (int j0 = 0; j0 < lr; j0 += 4)
       {
-        const int i = e / lr, j = e - i * lr;
-        M32[e] = j < n ? J32[i * n + j] * cf + (i == j ? 1.0f : 0.0f) : 0.0f;
+        float v0[4], v1[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+        {
+          const int j = j0 + u;
+          v0[u] = (j < n && lane < n) ? J32[j * n + lane] * cf + (lane == j ? 1.0f : 0.0f) : 0.0f;
+          v1[u] = (j < n && lane + 32 < n) ? J32[j * n + lane + 32] * cf + (lane + 32 == j ? 1.0f : 0.0f)
+                                           : 0.0f;
+        }
+        if (lane < n) *reinterpret_cast<float4*>(M32 + lane * lr + j0) = make_float4(v0[0], v0[1], v0[2], v0[3]);
+        if (lane + 32 < n)
+          *reinterpret_cast<float4*>(M32 + (lane + 32) * lr + j0) = make_float4(v1[0], v1[1], v1[2], v1[3]);
       }
       __syncwarp();
       lu = gauss_jordan(M32);
