@@ -1,0 +1,230 @@
+"""TEST ORACLE (checker only): CVODE runs of the 2-D heat problem of
+examples/cvode/CXX_serial/cv_heat2D.cpp -- 5-point stencil on the nx x ny
+interior grid, zero Dirichlet boundaries, no forcing term, BDF + Newton +
+SPGMR (left preconditioning, maxl 5) with the user J v and the Jacobi
+preconditioner (cv_heat2D.cpp:371-408) -- by two drivers:
+
+* ``run_reference``: the reference's own CVode and its NVECTOR_SERIAL /
+  SUNLINSOL_SPGMR objects (``oracle/_ref``, built where the reference sources
+  are present) with serial callbacks restated here in numpy;
+* ``run_port``: the C restatement ``oracle/cvode_ls_port.c`` (in
+  ``oracle/_build/liboracle.so``), which drives any N_Vector and
+  SUNLinearSolver through their ops tables -- the reference's serial objects
+  (to pin it against ``run_reference``) or NVECTOR_GB300 +
+  SUNLinSol_SPGMR_GB300 with the device callbacks of include/heat2d_gb300.h.
+
+Both return the counters after every output time (COUNTER_NAMES) and the
+solutions there."""
+from __future__ import annotations
+
+import ctypes as ct
+from pathlib import Path
+
+import numpy as np
+
+from . import heat2d_port as hp
+from . import port
+
+REF_LIB = Path(__file__).resolve().parent / "_ref" / "libsundials_ref.so"
+COUNTER_NAMES = ("nst", "nfe", "nni", "nnf", "ncfn", "netf", "nsetups", "nli", "npe", "nps",
+                 "njtimes", "ncfl", "qu", "q")
+REAL_NAMES = ("hu", "h", "tn", "h0u")
+
+VP, D, I, I64 = ct.c_void_p, ct.c_double, ct.c_int, ct.c_int64
+RHS_FN = ct.CFUNCTYPE(I, D, VP, VP, VP)
+JTIMES_FN = ct.CFUNCTYPE(I, VP, VP, D, VP, VP, VP, VP)
+PSETUP_FN = ct.CFUNCTYPE(I, D, VP, VP, I, ct.POINTER(I), D, VP)
+PSOLVE_FN = ct.CFUNCTYPE(I, D, VP, VP, VP, VP, D, D, I, VP)
+
+
+def initial(nx: int, ny: int, seed: int = 1) -> np.ndarray:
+    """u0 = sin(pi x) sin(pi y) + U(-1e-3, 1e-3) on the interior points, row by row."""
+    x = np.arange(1, nx + 1) / (nx + 1)
+    y = np.arange(1, ny + 1) / (ny + 1)
+    u = np.sin(np.pi * y)[:, None] * np.sin(np.pi * x)[None, :]
+    return (u + np.random.default_rng(seed).uniform(-1e-3, 1e-3, (ny, nx))).reshape(-1)
+
+
+def ref_lib() -> ct.CDLL:
+    L = ct.CDLL(str(REF_LIB))
+    for name, res, args in [
+        ("SUNContext_Create", I, [I, ct.POINTER(VP)]),
+        ("SUNContext_Free", I, [ct.POINTER(VP)]),
+        ("N_VNew_Serial", VP, [I64, VP]),
+        ("N_VDestroy", None, [VP]),
+        ("N_VGetArrayPointer", ct.POINTER(D), [VP]),
+        ("SUNLinSol_SPGMR", VP, [VP, I, I, VP]),
+        ("SUNLinSolFree", I, [VP]),
+        ("CVodeCreate", VP, [I, VP]),
+        ("CVodeInit", I, [VP, VP, D, VP]),
+        ("CVodeSStolerances", I, [VP, D, D]),
+        ("CVodeSetMaxNumSteps", I, [VP, ct.c_long]),
+        ("CVodeSetLinearSolver", I, [VP, VP, VP]),
+        ("CVodeSetJacTimes", I, [VP, VP, VP]),
+        ("CVodeSetPreconditioner", I, [VP, VP, VP]),
+        ("CVode", I, [VP, D, VP, ct.POINTER(D), I]),
+        ("CVodeFree", None, [ct.POINTER(VP)]),
+    ]:
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    for name in ("CVodeGetNumSteps", "CVodeGetNumRhsEvals", "CVodeGetNumNonlinSolvIters",
+                 "CVodeGetNumNonlinSolvConvFails", "CVodeGetNumStepSolveFails",
+                 "CVodeGetNumErrTestFails", "CVodeGetNumLinSolvSetups", "CVodeGetNumLinIters",
+                 "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves", "CVodeGetNumJtimesEvals",
+                 "CVodeGetNumLinConvFails"):
+        f = getattr(L, name)
+        f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
+    for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
+        f = getattr(L, name)
+        f.restype, f.argtypes = I, [VP, ct.POINTER(I)]
+    for name in ("CVodeGetLastStep", "CVodeGetCurrentStep", "CVodeGetCurrentTime",
+                 "CVodeGetActualInitStep"):
+        f = getattr(L, name)
+        f.restype, f.argtypes = I, [VP, ct.POINTER(D)]
+    return L
+
+
+def port_lib() -> ct.CDLL:
+    L = port.lib()
+    if not getattr(L, "_cvls_declared", False):
+        L.cvls_port_create.restype = VP
+        L.cvls_port_create.argtypes = [VP, D, VP, D, D, ct.c_long, VP, VP, VP, VP, VP]
+        L.cvls_port_solve.restype = I
+        L.cvls_port_solve.argtypes = [VP, D, VP, ct.POINTER(D)]
+        L.cvls_port_stats.restype = None
+        L.cvls_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
+        L.cvls_port_free.restype = None
+        L.cvls_port_free.argtypes = [VP]
+        L._cvls_declared = True
+    return L
+
+
+class SerialHeat:
+    """The problem's callbacks on NVECTOR_SERIAL vectors of the reference
+    library, rounded like the device callbacks (oracle/heat2d_port.py)."""
+
+    def __init__(self, L, nx: int, ny: int):
+        self.L, self.nx, self.ny, self.n = L, nx, ny, nx * ny
+        self.cc = hp.coefficients(nx, ny)[2]
+        self.d = 1.0
+
+        def arr(v):
+            return np.ctypeslib.as_array(L.N_VGetArrayPointer(v), shape=(self.n,))
+
+        def f(t, y, ydot, data):
+            arr(ydot)[:] = hp.jv(arr(y), nx, ny)
+            return 0
+
+        def jtimes(v, jv, t, y, fy, data, tmp):
+            arr(jv)[:] = hp.jv(arr(v), nx, ny)
+            return 0
+
+        def psetup(t, y, fy, jok, jcur, gamma, data):
+            self.d = 1.0 / (1.0 - gamma * self.cc)
+            return 0
+
+        def psolve(t, y, fy, r, z, gamma, delta, lr, data):
+            arr(z)[:] = self.d * arr(r)
+            return 0
+
+        self.cbs = (RHS_FN(f), JTIMES_FN(jtimes), PSETUP_FN(psetup), PSOLVE_FN(psolve))
+        self.arr = arr
+
+    def addresses(self):
+        return tuple(ct.cast(c, VP).value for c in self.cbs)
+
+
+def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000):
+    """The reference's CVode on serial vectors: (counters [len(touts), 14],
+    reals [len(touts), 4], solutions [len(touts), nx*ny], u0)."""
+    L = ref_lib()
+    ctx = VP()
+    assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
+    heat = SerialHeat(L, nx, ny)
+    u0 = initial(nx, ny)
+    y = L.N_VNew_Serial(heat.n, ctx)
+    heat.arr(y)[:] = u0
+    mem = L.CVodeCreate(2, ctx)
+    f, jt, ps, pv = heat.addresses()
+    assert L.CVodeInit(mem, f, 0.0, y) == 0
+    assert L.CVodeSStolerances(mem, rtol, atol) == 0
+    assert L.CVodeSetMaxNumSteps(mem, mxstep) == 0
+    LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+    assert L.CVodeSetLinearSolver(mem, LS, None) == 0
+    assert L.CVodeSetJacTimes(mem, None, jt) == 0
+    assert L.CVodeSetPreconditioner(mem, ps, pv) == 0
+    cnt, real, sols = [], [], []
+    t = D()
+    for tout in touts:
+        flag = L.CVode(mem, tout, y, ct.byref(t), 1)
+        assert flag == 0, flag
+        c, li, ri = ct.c_long(), I(), D()
+        row = []
+        for name in ("CVodeGetNumSteps", "CVodeGetNumRhsEvals", "CVodeGetNumNonlinSolvIters",
+                     "CVodeGetNumNonlinSolvConvFails", "CVodeGetNumStepSolveFails",
+                     "CVodeGetNumErrTestFails", "CVodeGetNumLinSolvSetups", "CVodeGetNumLinIters",
+                     "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves", "CVodeGetNumJtimesEvals",
+                     "CVodeGetNumLinConvFails"):
+            getattr(L, name)(mem, ct.byref(c))
+            row.append(c.value)
+        for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
+            getattr(L, name)(mem, ct.byref(li))
+            row.append(li.value)
+        rrow = []
+        for name in ("CVodeGetLastStep", "CVodeGetCurrentStep", "CVodeGetCurrentTime",
+                     "CVodeGetActualInitStep"):
+            getattr(L, name)(mem, ct.byref(ri))
+            rrow.append(ri.value)
+        cnt.append(row)
+        real.append(rrow)
+        sols.append(heat.arr(y).copy())
+    pm = VP(mem)
+    L.CVodeFree(ct.byref(pm))
+    L.SUNLinSolFree(LS)
+    L.N_VDestroy(y)
+    L.SUNContext_Free(ct.byref(ctx))
+    return np.array(cnt, np.int64), np.array(real), np.array(sols), u0
+
+
+def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000):
+    """The restated CVODE on whatever objects it is given: y0_handle (an
+    N_Vector holding u0, also used for the outputs), LS_handle (a
+    SUNLinearSolver built on it), callbacks = (f, jtimes, psetup, psolve,
+    user_data) addresses, get(handle) -> numpy copy of a vector."""
+    P = port_lib()
+    f, jt, ps, pv, data = callbacks
+    mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, ps, pv, data)
+    assert mem
+    cnt, real, sols = [], [], []
+    t = D()
+    c = (ct.c_long * 14)()
+    r = (D * 4)()
+    try:
+        for tout in touts:
+            flag = P.cvls_port_solve(mem, tout, y0_handle, ct.byref(t))
+            assert flag == 0, flag
+            P.cvls_port_stats(mem, c, r)
+            cnt.append(list(c))
+            real.append(list(r))
+            sols.append(get(y0_handle))
+    finally:
+        P.cvls_port_free(mem)
+    return np.array(cnt, np.int64), np.array(real), np.array(sols)
+
+
+def run_port_serial(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10):
+    """run_port on the reference's own serial vector and SPGMR (the pin)."""
+    L = ref_lib()
+    ctx = VP()
+    assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
+    heat = SerialHeat(L, nx, ny)
+    y = L.N_VNew_Serial(heat.n, ctx)
+    heat.arr(y)[:] = initial(nx, ny)
+    LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+    try:
+        return run_port(y, LS, heat.addresses() + (None,), lambda h: heat.arr(h).copy(), touts,
+                        rtol, atol)
+    finally:
+        L.SUNLinSolFree(LS)
+        L.N_VDestroy(y)
+        L.SUNContext_Free(ct.byref(ctx))

@@ -58,6 +58,14 @@ class Heat2D:
         return (addr("SUNHeat2D_GB300_ATimes"), addr("SUNHeat2D_GB300_PSetup"),
                 addr("SUNHeat2D_GB300_PSolve"), self.p)
 
+    def cvode_callbacks(self):
+        """(CVRhsFn, CVLsJacTimesVecFn, CVLsPrecSetupFn, CVLsPrecSolveFn)
+        addresses for CVodeInit / CVodeSetJacTimes / CVodeSetPreconditioner,
+        and the user-data pointer they take."""
+        addr = lambda name: ct.cast(getattr(self.lib, name), ct.c_void_p).value
+        return (addr("SUNHeat2D_GB300_RHS"), addr("SUNHeat2D_GB300_JTimes"),
+                addr("SUNHeat2D_GB300_CVPSetup"), addr("SUNHeat2D_GB300_CVPSolve"), self.p)
+
     def free(self) -> None:
         if self.p:
             self.lib.SUNHeat2D_GB300_Free(self.p)

@@ -1,0 +1,66 @@
+"""GPU: whole CVODE integrations of the 2-D heat problem with the GB300
+modules plugged in -- NVECTOR_GB300 for every vector, SUNLinSol_SPGMR_GB300
+(left Jacobi preconditioning, maxl 5, modified Gram-Schmidt) as the linear
+solver, the device callbacks of include/heat2d_gb300.h as f / J v / psetup /
+psolve -- driven by the CVODE restatement oracle/cvode_ls_port.c (the
+reference's CVode, bit for bit on serial objects: tests/test_cvode_ls_port.py)
+and compared with the reference's own run on NVECTOR_SERIAL + SUNLINSOL_SPGMR
+(tests/golden/heat_cvode_ref.npz).
+
+What differs from the serial objects is the summation order of the dot
+products and norms (a fixed tree instead of a sequential loop), the fused
+Gram-Schmidt kernels (deferred normalisation) and, with FMA on, one rounding
+per contracted product.  The bar: the integer counters of every output
+(steps, RHS evaluations, Newton and linear iterations, setups, failures)
+equal the reference's, and the solutions agree to 1e-3 * rtol in the
+weighted RMS norm of the run (CVODE's own error weights at the reference
+solution)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import heat_cvode as hc
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden" / "heat_cvode_ref.npz"
+
+
+def _run(name, fma, fused):
+    from sundials_gb300.heat2d import Heat2D
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.spgmr import PREC_LEFT, SPGMR
+    g = np.load(GOLDEN)
+    nx, ny = (int(v) for v in g[f"{name}_grid"])
+    rtol, atol = (float(v) for v in g[f"{name}_tol"])
+    touts = [float(t) for t in g[f"{name}_touts"]]
+    y = NVector.from_numpy(g[f"{name}_u0"])
+    y.set_fma(fma)
+    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    assert S.set_fused(fused) == 0
+    heat = Heat2D(nx, ny)
+    try:
+        c, r, s = hc.run_port(y.v, S.S, heat.cvode_callbacks(), lambda h: y.get(), touts, rtol,
+                              atol)
+    finally:
+        S.free()
+        heat.free()
+    return g, c, r, s, rtol, atol
+
+
+def _wrms(d, yref, rtol, atol):
+    w = 1.0 / (rtol * np.abs(yref) + atol)
+    return float(np.sqrt(np.mean((d * w) ** 2)))
+
+
+@pytest.mark.parametrize("name", ["g32", "g48x32_tight", "g128"])
+@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_cvode_heat_matches_reference(name, fused, fma):
+    g, c, r, s, rtol, atol = _run(name, fma, fused)
+    c_ref, y_ref = g[f"{name}_counters"], g[f"{name}_y"]
+    assert np.array_equal(c, c_ref), (c - c_ref).tolist()
+    for k in range(len(y_ref)):
+        assert _wrms(s[k] - y_ref[k], y_ref[k], rtol, atol) <= 1e-3 * rtol
+    # the time reached and the last step: same to rounding
+    np.testing.assert_allclose(r[:, :3], g[f"{name}_reals"][:, :3], rtol=1e-9)
