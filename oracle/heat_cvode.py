@@ -51,6 +51,7 @@ def ref_lib() -> ct.CDLL:
         ("SUNContext_Create", I, [I, ct.POINTER(VP)]),
         ("SUNContext_Free", I, [ct.POINTER(VP)]),
         ("N_VNew_Serial", VP, [I64, VP]),
+        ("N_VNew_OpenMP", VP, [I64, I, VP]),
         ("N_VDestroy", None, [VP]),
         ("N_VGetArrayPointer", ct.POINTER(D), [VP]),
         ("SUNLinSol_SPGMR", VP, [VP, I, I, VP]),
@@ -134,15 +135,17 @@ class SerialHeat:
         return tuple(ct.cast(c, VP).value for c in self.cbs)
 
 
-def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000):
-    """The reference's CVode on serial vectors: (counters [len(touts), 14],
-    reals [len(touts), 4], solutions [len(touts), nx*ny], u0)."""
+def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000, threads=None):
+    """The reference's CVode on serial vectors (or, with threads = k,
+    NVECTOR_OPENMP on k threads, whose reductions sum in another order):
+    (counters [len(touts), 14], reals [len(touts), 4], solutions
+    [len(touts), nx*ny], u0)."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
     heat = SerialHeat(L, nx, ny)
     u0 = initial(nx, ny)
-    y = L.N_VNew_Serial(heat.n, ctx)
+    y = L.N_VNew_Serial(heat.n, ctx) if threads is None else L.N_VNew_OpenMP(heat.n, threads, ctx)
     heat.arr(y)[:] = u0
     mem = L.CVodeCreate(2, ctx)
     f, jt, ps, pv = heat.addresses()

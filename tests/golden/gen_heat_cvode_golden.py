@@ -5,7 +5,13 @@ examples/cvode/CXX_serial/cv_heat2D.cpp (no forcing term; BDF, Newton, SPGMR
 with left Jacobi preconditioning, maxl 5, user J v), u0 = sin(pi x) sin(pi y)
 + U(-1e-3, 1e-3) (seed 1).  Per case: u0, the output times, the counters
 after each output (oracle/heat_cvode.py:COUNTER_NAMES), hu / h / tn / h0u and
-the solutions.
+the solutions; and the reference's own sensitivity to the summation order of
+its reductions: the same runs on NVECTOR_OPENMP with 2, 3, 4, 6, 8 and 16
+threads (counters after the last output, and the largest weighted RMS
+distance of their solutions from the serial ones, in units of the error
+tolerance).  OpenMP combines its per-thread partial sums in an order that may
+change from run to run, so these rows are a sample of that sensitivity, not
+values to reproduce.
 
 Usage (where the reference sources exist):
     python -m sundials_gb300.build && python tests/golden/gen_heat_cvode_golden.py
@@ -20,6 +26,7 @@ sys.path.insert(0, str(ROOT))
 from oracle import heat_cvode as hc  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "heat_cvode_ref.npz"
+THREADS = (2, 3, 4, 6, 8, 16)
 
 # name: (nx, ny, rtol, atol, output times)
 CASES = {
@@ -41,6 +48,19 @@ def main():
         out[f"{name}_reals"] = r
         out[f"{name}_y"] = s
         print(name, dict(zip(hc.COUNTER_NAMES, c[-1].tolist())))
+        oc, ow = [], []
+        for th in THREADS:
+            c2, _, s2, _ = hc.run_reference(nx, ny, touts, rtol, atol, threads=th)
+            w = 1.0 / (rtol * np.abs(s) + atol)
+            oc.append(c2[-1])
+            ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))
+        out[f"{name}_omp_threads"] = np.array(THREADS)
+        out[f"{name}_omp_counters"] = np.array(oc, np.int64)
+        out[f"{name}_omp_wrms"] = np.array(ow)
+        print("   order sensitivity:", {n: (int(np.min(np.array(oc)[:, k] - c[-1][k])),
+                                            int(np.max(np.array(oc)[:, k] - c[-1][k])))
+                                        for k, n in enumerate(hc.COUNTER_NAMES)},
+              "wrms", max(ow))
     np.savez_compressed(OUT, names=np.array(list(CASES)), **out)
     print("wrote", OUT)
 
