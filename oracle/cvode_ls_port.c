@@ -15,7 +15,7 @@
  * Follows, in the same floating-point order (compiled with -ffp-contract=off):
  *   CVode, CV_NORMAL (no tstop, roots, constraints or projection)
  *                                  src/cvode/cvode.c:1037-1640
- *   cvEwtSetSS                     cvode.c:4791-4830
+ *   cvEwtSetSS / cvEwtSetSV        cvode.c:4791-4860
  *   cvHin / cvUpperBoundH0 / cvYddNorm   cvode.c:2161-2340
  *   cvStep and its callees         cvode.c:2367-3727
  *   CVodeGetDky (k = 0)            cvode.c:1671-1750
@@ -102,6 +102,7 @@ typedef struct
   /* vectors */
   N_Vector zn[QMAX + 1], ewt, acor, tempv, ftemp, y, delta, ls_x, ls_ytemp;
   N_Vector ycur, fcur; /* CVLS's pointers to the current state and RHS */
+  N_Vector Vabstol;    /* CVodeSVtolerances' copy, or NULL for scalar atol */
   /* CVLS */
   double nrmfac, eplifac;
   sunbooleantype jbad;
@@ -153,13 +154,17 @@ static void v_scalevectorarray(int nvec, double* c, N_Vector* X, N_Vector* Z)
     for (int i = 0; i < nvec; i++) Z[0]->ops->nvscale(c[i], X[i], Z[i]);
 }
 
-/* cvEwtSetSS (atol > 0, so no N_VMin test) */
+/* cvEwtSetSS / cvEwtSetSV (absolute tolerances > 0, so no N_VMin test) */
 static void set_ewt(CvlsPort* m, N_Vector ycur, N_Vector w)
 {
   N_Vector t = m->tempv;
   t->ops->nvabs(ycur, t);
-  v_scale(m->rtol, t, t);
-  t->ops->nvaddconst(t, m->atol, t);
+  if (m->Vabstol) v_linearsum(m->rtol, t, 1.0, m->Vabstol, t);
+  else
+  {
+    v_scale(m->rtol, t, t);
+    t->ops->nvaddconst(t, m->atol, t);
+  }
   t->ops->nvinv(t, w);
 }
 
@@ -890,6 +895,15 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   return m;
 }
 
+/* CVodeSVtolerances(rtol, abstol): a copy of abstol is kept (all entries > 0). */
+void cvls_port_set_vabstol(void* mem, double rtol, N_Vector abstol)
+{
+  CvlsPort* m = (CvlsPort*)mem;
+  m->rtol     = rtol;
+  if (!m->Vabstol) m->Vabstol = abstol->ops->nvclone(abstol);
+  v_scale(1.0, abstol, m->Vabstol);
+}
+
 /* One CVode(tout, yout, &tret, CV_NORMAL) call; returns the CVODE flag. */
 int cvls_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 {
@@ -991,5 +1005,6 @@ void cvls_port_free(void* mem)
   N_Vector vs[] = {m->ewt, m->acor, m->tempv, m->ftemp, m->y, m->delta, m->ls_ytemp, m->ls_x};
   for (int i = 0; i < (int)(sizeof(vs) / sizeof(vs[0])); i++) vs[i]->ops->nvdestroy(vs[i]);
   for (int j = 0; j <= QMAX; j++) m->zn[j]->ops->nvdestroy(m->zn[j]);
+  if (m->Vabstol) m->Vabstol->ops->nvdestroy(m->Vabstol);
   free(m);
 }

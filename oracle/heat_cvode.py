@@ -1,4 +1,6 @@
-"""TEST ORACLE (checker only): CVODE runs of the 2-D heat problem of
+"""TEST ORACLE (checker only): CVODE runs of user problems with SPGMR
+(``run_reference_with`` / ``run_port`` / ``run_port_serial_with``, used by
+oracle/robertson_cvode.py too), and the 2-D heat problem of
 examples/cvode/CXX_serial/cv_heat2D.cpp -- 5-point stencil on the nx x ny
 interior grid, zero Dirichlet boundaries, no forcing term, BDF + Newton +
 SPGMR (left preconditioning, maxl 5) with the user J v and the Jacobi
@@ -59,6 +61,7 @@ def ref_lib() -> ct.CDLL:
         ("CVodeCreate", VP, [I, VP]),
         ("CVodeInit", I, [VP, VP, D, VP]),
         ("CVodeSStolerances", I, [VP, D, D]),
+        ("CVodeSVtolerances", I, [VP, D, VP]),
         ("CVodeSetMaxNumSteps", I, [VP, ct.c_long]),
         ("CVodeSetLinearSolver", I, [VP, VP, VP]),
         ("CVodeSetJacTimes", I, [VP, VP, VP]),
@@ -96,6 +99,8 @@ def port_lib() -> ct.CDLL:
         L.cvls_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
         L.cvls_port_free.restype = None
         L.cvls_port_free.argtypes = [VP]
+        L.cvls_port_set_vabstol.restype = None
+        L.cvls_port_set_vabstol.argtypes = [VP, D, VP]
         L._cvls_declared = True
     return L
 
@@ -136,21 +141,39 @@ class SerialHeat:
 
 
 def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000, threads=None):
-    """The reference's CVode on serial vectors (or, with threads = k,
-    NVECTOR_OPENMP on k threads, whose reductions sum in another order):
-    (counters [len(touts), 14], reals [len(touts), 4], solutions
-    [len(touts), nx*ny], u0)."""
+    """The reference's CVode on the heat problem with serial vectors (or,
+    with threads = k, NVECTOR_OPENMP on k threads, whose reductions sum in
+    another order): (counters [len(touts), 14], reals [len(touts), 4],
+    solutions [len(touts), nx*ny], u0)."""
+    u0 = initial(nx, ny)
+    c, r, s = run_reference_with(lambda L: SerialHeat(L, nx, ny), u0, touts, rtol, atol, mxstep,
+                                 threads)
+    return c, r, s, u0
+
+
+def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, threads=None):
+    """The reference's CVode (BDF, Newton, SPGMR with left preconditioning and
+    maxl 5, user J v and preconditioner) on the problem whose serial
+    callbacks make_serial(L) builds (an object with .addresses() -> (f,
+    jtimes, psetup, psolve) and .arr(N_Vector) -> numpy view).  atol: a
+    scalar (CVodeSStolerances) or an array (CVodeSVtolerances)."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
-    heat = SerialHeat(L, nx, ny)
-    u0 = initial(nx, ny)
-    y = L.N_VNew_Serial(heat.n, ctx) if threads is None else L.N_VNew_OpenMP(heat.n, threads, ctx)
-    heat.arr(y)[:] = u0
+    prob = make_serial(L)
+    n = len(u0)
+    y = L.N_VNew_Serial(n, ctx) if threads is None else L.N_VNew_OpenMP(n, threads, ctx)
+    prob.arr(y)[:] = u0
     mem = L.CVodeCreate(2, ctx)
-    f, jt, ps, pv = heat.addresses()
+    f, jt, ps, pv = prob.addresses()
     assert L.CVodeInit(mem, f, 0.0, y) == 0
-    assert L.CVodeSStolerances(mem, rtol, atol) == 0
+    vatol = None
+    if np.ndim(atol) == 0:
+        assert L.CVodeSStolerances(mem, rtol, atol) == 0
+    else:
+        vatol = L.N_VNew_Serial(n, ctx)
+        prob.arr(vatol)[:] = atol
+        assert L.CVodeSVtolerances(mem, rtol, vatol) == 0
     assert L.CVodeSetMaxNumSteps(mem, mxstep) == 0
     LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
     assert L.CVodeSetLinearSolver(mem, LS, None) == 0
@@ -180,24 +203,31 @@ def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
             rrow.append(ri.value)
         cnt.append(row)
         real.append(rrow)
-        sols.append(heat.arr(y).copy())
+        sols.append(prob.arr(y).copy())
     pm = VP(mem)
     L.CVodeFree(ct.byref(pm))
     L.SUNLinSolFree(LS)
     L.N_VDestroy(y)
+    if vatol:
+        L.N_VDestroy(vatol)
     L.SUNContext_Free(ct.byref(ctx))
-    return np.array(cnt, np.int64), np.array(real), np.array(sols), u0
+    return np.array(cnt, np.int64), np.array(real), np.array(sols)
 
 
-def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000):
+def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
+             vatol_handle=None):
     """The restated CVODE on whatever objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (f, jtimes, psetup, psolve,
-    user_data) addresses, get(handle) -> numpy copy of a vector."""
+    user_data) addresses, get(handle) -> numpy copy of a vector;
+    vatol_handle: an N_Vector of absolute tolerances (else atol, a scalar)."""
     P = port_lib()
     f, jt, ps, pv, data = callbacks
-    mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, ps, pv, data)
+    mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, 0.0 if vatol_handle else atol, mxstep,
+                             LS_handle, jt, ps, pv, data)
     assert mem
+    if vatol_handle:
+        P.cvls_port_set_vabstol(mem, rtol, vatol_handle)
     cnt, real, sols = [], [], []
     t = D()
     c = (ct.c_long * 14)()
@@ -217,17 +247,28 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
 
 def run_port_serial(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10):
     """run_port on the reference's own serial vector and SPGMR (the pin)."""
+    return run_port_serial_with(lambda L: SerialHeat(L, nx, ny), initial(nx, ny), touts, rtol,
+                                atol)
+
+
+def run_port_serial_with(make_serial, u0, touts, rtol, atol):
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
-    heat = SerialHeat(L, nx, ny)
-    y = L.N_VNew_Serial(heat.n, ctx)
-    heat.arr(y)[:] = initial(nx, ny)
+    prob = make_serial(L)
+    y = L.N_VNew_Serial(len(u0), ctx)
+    prob.arr(y)[:] = u0
     LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+    vatol = None
+    if np.ndim(atol) != 0:
+        vatol = L.N_VNew_Serial(len(u0), ctx)
+        prob.arr(vatol)[:] = atol
     try:
-        return run_port(y, LS, heat.addresses() + (None,), lambda h: heat.arr(h).copy(), touts,
-                        rtol, atol)
+        return run_port(y, LS, prob.addresses() + (None,), lambda h: prob.arr(h).copy(), touts,
+                        rtol, atol, vatol_handle=vatol)
     finally:
         L.SUNLinSolFree(LS)
         L.N_VDestroy(y)
+        if vatol:
+            L.N_VDestroy(vatol)
         L.SUNContext_Free(ct.byref(ctx))

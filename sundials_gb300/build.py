@@ -47,6 +47,7 @@ PER_FILE_FLAGS = {
     # host-side Givens QR and norm tests rounded like the reference's C
     "sunlinsol_spgmr_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "heat2d_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "robertson_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

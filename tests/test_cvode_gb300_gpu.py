@@ -1,11 +1,14 @@
-"""GPU: whole CVODE integrations of the 2-D heat problem with the GB300
-modules plugged in -- NVECTOR_GB300 for every vector, SUNLinSol_SPGMR_GB300
-(left Jacobi preconditioning, maxl 5, modified Gram-Schmidt) as the linear
-solver, the device callbacks of include/heat2d_gb300.h as f / J v / psetup /
-psolve -- driven by the CVODE restatement oracle/cvode_ls_port.c (the
-reference's CVode, bit for bit on serial objects: tests/test_cvode_ls_port.py)
-and compared with the reference's own run on NVECTOR_SERIAL + SUNLINSOL_SPGMR
-(tests/golden/heat_cvode_ref.npz).
+"""GPU: whole CVODE integrations with the GB300 modules plugged in --
+NVECTOR_GB300 for every vector, SUNLinSol_SPGMR_GB300 (left preconditioning,
+maxl 5, modified Gram-Schmidt) as the linear solver, and device callbacks as
+f / J v / psetup / psolve: the 2-D heat problem with its Jacobi
+preconditioner (include/heat2d_gb300.h), and the batched Robertson problem
+with the exact block-Jacobi preconditioner on SUNLinSol_BlockLU_GB300
+(include/robertson_gb300.h) -- driven by the CVODE restatement
+oracle/cvode_ls_port.c (the reference's CVode, bit for bit on serial objects:
+tests/test_cvode_ls_port.py, tests/test_robertson_cvode.py) and compared with
+the reference's own runs on NVECTOR_SERIAL + SUNLINSOL_SPGMR
+(tests/golden/heat_cvode_ref.npz, robertson_cvode_ref.npz).
 
 What differs from the serial objects is the summation order of the dot
 products and norms (a fixed tree instead of a sequential loop), the fused
@@ -75,3 +78,67 @@ def test_cvode_heat_matches_reference(name, fused, fma):
     for k in range(len(y_ref)):
         w = _wrms(s[k] - y_ref[k], y_ref[k], rtol, atol)
         assert w <= 3.0 * own_wrms and w <= 10.0, (k, w, own_wrms)
+
+
+ROB_GOLDEN = Path(__file__).resolve().parent / "golden" / "robertson_cvode_ref.npz"
+
+
+def _run_robertson(name, fma, fused, lu):
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.robertson import Robertson
+    from sundials_gb300.spgmr import PREC_LEFT, SPGMR
+    from oracle import robertson_cvode as rc
+    g = np.load(ROB_GOLDEN)
+    k = g[f"{name}_k"]
+    ncells = len(k)
+    y = NVector.from_numpy(rc.initial(ncells))
+    y.set_fma(fma)
+    vatol = NVector.from_numpy(rc.vector_atol(ncells))
+    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    assert S.set_fused(fused) == 0
+    prob = Robertson(k, y, lu)
+    try:
+        c, r, s = hc.run_port(y.v, S.S, prob.cvode_callbacks(), lambda h: y.get(),
+                              [float(t) for t in g[f"{name}_touts"]], float(g[f"{name}_rtol"]),
+                              0.0, vatol_handle=vatol.v)
+    finally:
+        S.free()
+        prob.free()
+    return g, c, r, s
+
+
+@pytest.mark.parametrize("name", ["r256", "r1024"])
+@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_cvode_robertson_block_preconditioner_matches_reference(name, fused, fma):
+    """FP64 block LU (bit-identical to SUNDlsMat_denseGETRF/GETRS per block):
+    the reference's own summation-order runs never moved a counter here, so
+    every counter after every output must equal the reference's."""
+    from oracle import robertson_cvode as rc
+    from sundials_gb300.robertson import LU_FP64
+    g, c, r, s = _run_robertson(name, fma, fused, LU_FP64)
+    assert np.array_equal(c, g[f"{name}_counters"]), (c[-1] - g[f"{name}_counters"][-1]).tolist()
+    rtol = float(g[f"{name}_rtol"])
+    atol = rc.vector_atol(len(g[f"{name}_k"]))
+    own = float(g[f"{name}_omp_wrms"].max())
+    for j, k in enumerate(g[f"{name}_y_index"]):
+        yr = g[f"{name}_y"][j]
+        w = float(np.sqrt(np.mean(((s[k] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+        assert w <= max(3.0 * own, 1e-6) and w <= 10.0, (k, w, own)
+
+
+def test_cvode_robertson_mixed_block_preconditioner():
+    """The FP32-inverse + FP64-refinement block LU as the preconditioner: a
+    different (approximate) preconditioner, so SPGMR's iteration counts may
+    move; the integration must keep the reference's step count within 5% and
+    its solution within the error tolerance."""
+    from oracle import robertson_cvode as rc
+    from sundials_gb300.robertson import LU_MIXED
+    g, c, r, s = _run_robertson("r1024", True, True, LU_MIXED)
+    cr = g["r1024_counters"][-1]
+    assert abs(int(c[-1][0]) - int(cr[0])) <= 0.05 * cr[0]
+    atol = rc.vector_atol(1024)
+    for j, k in enumerate(g["r1024_y_index"]):
+        yr = g["r1024_y"][j]
+        w = float(np.sqrt(np.mean(((s[k] - yr) / (1e-4 * np.abs(yr) + atol)) ** 2)))
+        assert w <= 1.0, (k, w)
