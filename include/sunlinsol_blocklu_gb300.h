@@ -30,8 +30,15 @@
  *   SUNBLOCKLU_MIXED  FP32 inverse of each block (Gauss-Jordan with partial
  *                     pivoting), applied in FP32 and refined once in FP64
  *                     against the FP64 matrix, which setup leaves intact.
+ *                     Setup probes each inverse X with two vectors v
+ *                     (|v - X A v|_inf <= 1/4, i.e. the refinement contracts);
+ *                     a block that fails the probe, or meets a zero pivot in
+ *                     FP32, is factored by the FP64 path instead (a copy of
+ *                     it, in storage allocated on first need) and solved
+ *                     exactly as SUNBLOCKLU_FP64 solves it.
  * Setup returns SUNLS_LUFACT_FAIL (recoverable) if any block has a zero
- * pivot; SUNLinSolLastFlag then gives 1 + the global column of the first one.
+ * pivot in FP64; SUNLinSolLastFlag then gives 1 + the global column of the
+ * first one.
  * ------------------------------------------------------------------------- */
 #ifndef SUNLINSOL_BLOCKLU_GB300_H
 #define SUNLINSOL_BLOCKLU_GB300_H

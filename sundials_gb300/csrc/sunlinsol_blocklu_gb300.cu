@@ -307,7 +307,7 @@ __global__ void k_bd_getrs_warp(const double* data, const int64_t* off, const in
 // FP32 inverse of each block by Gauss-Jordan with partial pivoting (one warp
 // per block, any size <= 64), written to inv (boff layout).
 __global__ void k_bd_inv32(const double* data, const int64_t* off, const int64_t* boff,
-                           int64_t nblocks, float* inv, unsigned long long* flag)
+                           int64_t nblocks, float* inv, uint8_t* fb_mark)
 {
   const int lane  = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -347,8 +347,8 @@ __global__ void k_bd_inv32(const double* data, const int64_t* off, const int64_t
         }
       }
       if (bk == 0)
-      {
-        if (lane == 0) atomicMin(flag, (unsigned long long)(off[b] + k + 1));
+      {  // singular in FP32: the block is factored in FP64 instead
+        if (lane == 0) fb_mark[b] = 1;
         failed = true;
         break;
       }
@@ -394,15 +394,89 @@ __global__ void k_bd_inv32(const double* data, const int64_t* off, const int64_t
   }
 }
 
-// x = inv b (FP32), r = b - A x (FP64), x += inv r (FP32 apply); x holds b.
-__global__ void k_bd_solve_mixed(const double* data, const float* inv, const int64_t* off,
-                                 const int64_t* boff, int64_t nblocks, double* x)
+// Quality probe of each FP32 inverse X: d = v - X (A v) for v = (1, 1, ...)
+// and v = (1, -1, 1, ...), A v in FP64.  One refinement sweep contracts the
+// error by about |I - X A|; blocks where |d|_inf > 1/4 (ill-conditioned
+// beyond FP32, |A| |A^-1| u32 >~ 1) -- or where the FP32 elimination met a
+// zero pivot -- are listed for an FP64 LU (the reference's GETRF/GETRS).
+__global__ void k_bd_probe32(const double* data, const float* inv, const int64_t* off,
+                             const int64_t* boff, int64_t nblocks, uint8_t* fb_mark,
+                             int32_t* fb_ids, unsigned* fb_count)
 {
   const int lane  = threadIdx.x & 31;
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t b = w; b < nblocks; b += W)
   {
+    bool bad = fb_mark[b] != 0;
+    if (!bad)
+    {
+      const int n     = (int)(off[b + 1] - off[b]);
+      const double* A = data + boff[b];
+      const float* V  = inv + boff[b];
+      double worst    = 0.0;
+      for (int alt = 0; alt < 2; alt++)
+      {
+        // t = A v (rows lane, lane + 32)
+        double t0 = 0.0, t1 = 0.0;
+        for (int j = 0; j < n; j++)
+        {
+          const double vj = (alt && (j & 1)) ? -1.0 : 1.0;
+          if (lane < n) t0 = fma(A[j * n + lane], vj, t0);
+          if (lane + 32 < n) t1 = fma(A[j * n + lane + 32], vj, t1);
+        }
+        const float c0 = (float)t0, c1 = (float)t1;
+        float u0 = 0.f, u1 = 0.f;
+        for (int j = 0; j < n; j++)
+        {
+          const float tj = __shfl_sync(0xffffffffu, j < 32 ? c0 : c1, j & 31);
+          if (lane < n) u0 = fmaf(V[j * n + lane], tj, u0);
+          if (lane + 32 < n) u1 = fmaf(V[j * n + lane + 32], tj, u1);
+        }
+        const double v0 = (alt && (lane & 1)) ? -1.0 : 1.0;
+        const double v1 = (alt && ((lane + 32) & 1)) ? -1.0 : 1.0;
+        double d = 0.0;
+        if (lane < n) d = fabs(v0 - (double)u0);
+        if (lane + 32 < n) d = fmax(d, fabs(v1 - (double)u1));
+        if (!(d <= 0.25)) d = 1.0e300;  // NaN or too large
+        worst = fmax(worst, d);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) worst = fmax(worst, __shfl_xor_sync(0xffffffffu, worst, o));
+      bad = worst > 0.25;
+      if (bad && lane == 0) fb_mark[b] = 1;
+    }
+    if (bad && lane == 0) fb_ids[atomicAdd(fb_count, 1u)] = (int32_t)b;
+  }
+}
+
+// Copy the listed blocks of A into lu (same layout) for their FP64 LU.
+__global__ void k_bd_copy_blocks(const double* data, const int64_t* off, const int64_t* boff,
+                                 const int32_t* ids, int64_t count, double* lu)
+{
+  const int lane  = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t t = w; t < count; t += W)
+  {
+    const int64_t b = ids[t];
+    const int n     = (int)(off[b + 1] - off[b]);
+    for (int e = lane; e < n * n; e += 32) lu[boff[b] + e] = data[boff[b] + e];
+  }
+}
+
+// x = inv b (FP32), r = b - A x (FP64), x += inv r (FP32 apply); x holds b.
+// Blocks marked for the FP64 fallback are left to k_bd_getrs_warp.
+__global__ void k_bd_solve_mixed(const double* data, const float* inv, const int64_t* off,
+                                 const int64_t* boff, int64_t nblocks, const uint8_t* fb_mark,
+                                 double* x)
+{
+  const int lane  = threadIdx.x & 31;
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t W = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t b = w; b < nblocks; b += W)
+  {
+    if (fb_mark[b]) continue;
     const int n     = (int)(off[b + 1] - off[b]);
     const double* A = data + boff[b];
     const float* V  = inv + boff[b];
@@ -510,6 +584,12 @@ struct LSContent
   int precision;
   int32_t* d_piv;                 // [N]
   float* d_inv;                   // [nnz] (MIXED)
+  uint8_t* d_fb_mark;             // [nblocks] (MIXED): block factored in FP64
+  int32_t* d_fb_ids;              // [nblocks] (MIXED): those blocks
+  unsigned* d_fb_count;           // (MIXED)
+  unsigned* h_fb_count;           // pinned
+  double* d_lu64;                 // [nnz] (MIXED, allocated on first use): their FP64 LU
+  int64_t fb_count, nblocks;
   unsigned long long* d_flag;     // first zero pivot: global column + 1
   unsigned long long* h_flag;     // pinned
   sunindextype last_flag;
@@ -677,6 +757,14 @@ SUNLinearSolver SUNLinSol_BlockLU_GB300(N_Vector y, SUNMatrix A, int precision, 
   c->nnz            = a->nnz;
   c->d_piv          = dalloc<int32_t>(a->N);
   c->d_inv          = precision == SUNBLOCKLU_MIXED ? dalloc<float>(a->nnz) : nullptr;
+  c->nblocks        = a->nblocks;
+  if (precision == SUNBLOCKLU_MIXED)
+  {
+    c->d_fb_mark  = dalloc<uint8_t>(a->nblocks);
+    c->d_fb_ids   = dalloc<int32_t>(a->nblocks);
+    c->d_fb_count = dalloc<unsigned>(1);
+    cudaHostAlloc(&c->h_fb_count, sizeof(unsigned), cudaHostAllocDefault);
+  }
   c->d_flag         = dalloc<unsigned long long>(1);
   cudaHostAlloc(&c->h_flag, sizeof(unsigned long long), cudaHostAllocDefault);
   return S;
@@ -699,9 +787,37 @@ int SUNLinSolSetup_BlockLU_GB300(SUNLinearSolver S, SUNMatrix A)
   cudaMemcpyAsync(c->d_flag, &none, sizeof none, cudaMemcpyHostToDevice, s);
   if (c->precision == SUNBLOCKLU_MIXED)
   {
+    cudaMemsetAsync(c->d_fb_mark, 0, a->nblocks, s);
+    cudaMemsetAsync(c->d_fb_count, 0, sizeof(unsigned), s);
     k_bd_inv32<<<warp_grid(a->nblocks), kBlock, 0, s>>>(a->d_data, a->d_off, a->d_boff,
-                                                         a->nblocks, c->d_inv, c->d_flag);
+                                                         a->nblocks, c->d_inv, c->d_fb_mark);
+    k_bd_probe32<<<warp_grid(a->nblocks), kBlock, 0, s>>>(a->d_data, c->d_inv, a->d_off,
+                                                           a->d_boff, a->nblocks, c->d_fb_mark,
+                                                           c->d_fb_ids, c->d_fb_count);
     count_launch();
+    count_launch();
+    cudaMemcpyAsync(c->h_fb_count, c->d_fb_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (!check_cuda(cudaStreamSynchronize(s), "SUNLinSolSetup_BlockLU_GB300"))
+    {
+      c->last_flag = SUN_ERR_EXT_FAIL;
+      return SUN_ERR_EXT_FAIL;
+    }
+    c->fb_count = *c->h_fb_count;
+    if (c->fb_count > 0)
+    {  // FP64 LU of the blocks the FP32 inverse cannot serve
+      if (!c->d_lu64) c->d_lu64 = dalloc<double>(a->nnz);
+      if (!c->d_lu64)
+      {
+        c->last_flag = SUN_ERR_MEM_FAIL;
+        return SUN_ERR_MEM_FAIL;
+      }
+      k_bd_copy_blocks<<<warp_grid(c->fb_count), kBlock, 0, s>>>(
+        a->d_data, a->d_off, a->d_boff, c->d_fb_ids, c->fb_count, c->d_lu64);
+      k_bd_getrf_warp<<<warp_grid(c->fb_count), kBlock, 0, s>>>(
+        c->d_lu64, a->d_off, a->d_boff, c->d_fb_ids, c->fb_count, c->d_piv, c->d_flag);
+      count_launch();
+      count_launch();
+    }
   }
   else
   {
@@ -745,9 +861,15 @@ int SUNLinSolSolve_BlockLU_GB300(SUNLinearSolver S, SUNMatrix A, N_Vector x, N_V
                     cudaMemcpyDeviceToDevice, s);
   if (c->precision == SUNBLOCKLU_MIXED)
   {
-    k_bd_solve_mixed<<<warp_grid(a->nblocks), kBlock, 0, s>>>(a->d_data, c->d_inv, a->d_off,
-                                                               a->d_boff, a->nblocks, xd);
+    k_bd_solve_mixed<<<warp_grid(a->nblocks), kBlock, 0, s>>>(
+      a->d_data, c->d_inv, a->d_off, a->d_boff, a->nblocks, c->d_fb_mark, xd);
     count_launch();
+    if (c->fb_count > 0)
+    {
+      k_bd_getrs_warp<<<warp_grid(c->fb_count), kBlock, 0, s>>>(
+        c->d_lu64, a->d_off, a->d_boff, c->d_fb_ids, c->fb_count, c->d_piv, xd);
+      count_launch();
+    }
   }
   else
   {
@@ -782,6 +904,11 @@ SUNErrCode SUNLinSolFree_BlockLU_GB300(SUNLinearSolver S)
     cudaFree(c->d_inv);
     cudaFree(c->d_flag);
     cudaFreeHost(c->h_flag);
+    cudaFree(c->d_fb_mark);
+    cudaFree(c->d_fb_ids);
+    cudaFree(c->d_fb_count);
+    cudaFreeHost(c->h_fb_count);
+    cudaFree(c->d_lu64);
     free(c);
   }
   free(S->ops);

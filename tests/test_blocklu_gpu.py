@@ -91,6 +91,48 @@ def test_mixed_solve_accuracy(gb300_lib):
     S.free()
 
 
+def test_mixed_falls_back_to_fp64_for_ill_conditioned_blocks(gb300_lib, port):
+    """Newton matrices I - gamma J of Robertson cells late in an integration
+    (gamma ~ 1e9, condition ~ 1e13, beyond FP32) among well-conditioned
+    blocks: the ill-conditioned ones fail the setup's probe and are factored
+    and solved by the FP64 path -- bit for bit SUNDlsMat_denseGETRF/GETRS --
+    while the others keep the FP32 inverse (accurate to refinement level)."""
+    rng = np.random.default_rng(8)
+    sizes = [3] * 40
+    blocks = []
+    ill = set(range(0, 40, 3))
+    for k in range(40):
+        if k in ill:
+            k1, k2, k3 = 0.04, 3e7, 1e4
+            y2, y3 = 1e-12 * rng.uniform(1, 2), rng.uniform(0.5, 1.0)
+            J = np.array([[-k1, k3 * y3, k3 * y2],
+                          [k1, -k3 * y3 - 2 * k2 * y2, -k3 * y2],
+                          [0.0, 2 * k2 * y2, 0.0]])
+            blocks.append(np.eye(3) - 1e9 * rng.uniform(1, 3) * J)
+        else:
+            blocks.append(np.eye(3) * 4.0 + rng.uniform(-1, 1, (3, 3)))
+    M = BD.BlockDiag(sizes)
+    M.set_blocks(blocks)
+    N = 3 * 40
+    b = rng.uniform(-1, 1, N)
+    X, B = exact_vec(np.zeros(N)), exact_vec(b)
+    S = BD.BlockLU(B.v, M, BD.MIXED)
+    assert S.setup(S.S, M.A) == 0
+    assert S.solve(S.S, M.A, X.v, B.v, 0.0) == 0
+    x = X.get()
+    for k, a in enumerate(blocks):
+        xs, bs = x[3 * k:3 * k + 3], b[3 * k:3 * k + 3]
+        if k in ill:
+            rl, rp, flag = port.dense_lu(a.T.copy())
+            assert flag == 0
+            assert beq(xs, port.dense_solve(rl, rp, bs)), k
+        else:
+            assert np.max(np.abs(a @ xs - bs)) <= 1e-10 * np.max(np.abs(bs)), k
+    for k, a in enumerate(M.get_blocks()):  # the matrix is still left intact
+        assert beq(a, blocks[k])
+    S.free()
+
+
 @pytest.mark.parametrize("precision", [BD.FP64, BD.MIXED])
 def test_zero_pivot_is_recoverable_failure(gb300_lib, precision):
     sizes = [3, 4, 40]

@@ -128,10 +128,12 @@ def test_cvode_robertson_block_preconditioner_matches_reference(name, fused, fma
 
 
 def test_cvode_robertson_mixed_block_preconditioner():
-    """The FP32-inverse + FP64-refinement block LU as the preconditioner: a
-    different (approximate) preconditioner, so SPGMR's iteration counts may
-    move; the integration must keep the reference's step count within 5% and
-    its solution within the error tolerance."""
+    """The FP32-inverse + FP64-refinement block LU as the preconditioner.  Late
+    in the run (t -> 4e10, gamma ~ 1e9) the Newton matrices' condition
+    numbers (~1e13) exceed what an FP32 inverse can serve; those blocks fail
+    the setup's probe and are factored in FP64.  The integration keeps the
+    reference's step count within 5% and its solutions within the error
+    tolerance at every stored output."""
     from oracle import robertson_cvode as rc
     from sundials_gb300.robertson import LU_MIXED
     g, c, r, s = _run_robertson("r1024", True, True, LU_MIXED)
