@@ -22,7 +22,7 @@
  *   cvNlsResidual / LSetup / LSolve / ConvTest   src/cvode/cvode_nls.c:256-398
  *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-330
  *   CVodeSetLinearSolver defaults for a matrix-free iterative solver,
- *   cvLsATimes / cvLsPSetup / cvLsPSolve, cvLsSetup, cvLsSolve
+ *   cvLsATimes / cvLsDQJtimes / cvLsPSetup / cvLsPSolve, cvLsSetup, cvLsSolve
  *                                  src/cvode/cvode_ls.c:56-285, 895-980, 1536-1900
  *   N_VLinearCombination / N_VScaleAddMulti / N_VScaleVectorArray dispatch
  *                                  src/sundials/sundials_nvector.c:549-670
@@ -106,7 +106,7 @@ typedef struct
   /* CVLS */
   double nrmfac, eplifac;
   sunbooleantype jbad;
-  long nstlj, npe, nli, nps, ncfl, njtimes;
+  long nstlj, npe, nli, nps, ncfl, njtimes, nfeDQ;
   int initialized;
   /* Newton */
   int curiter;
@@ -176,10 +176,33 @@ static int rhs(CvlsPort* m, double t, N_Vector y, N_Vector f)
 }
 
 /* ------------------------------------------------------ CVLS callbacks */
+/* cvLsDQJtimes (cvode_ls.c:1266-1305): Jv = (f(t, y + sig v) - fy) / sig,
+ * sig = 1 / |v|_wrms, shrunk by 1/4 on a recoverable f failure (3 tries) */
+static int dq_jtimes(CvlsPort* m, N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vector fy,
+                     N_Vector work)
+{
+  double sig = 1.0 / v_wrms(v, m->ewt);
+  int retval = 0;
+  for (int iter = 0; iter < 3; iter++)
+  {
+    v_linearsum(sig, v, 1.0, y, work);
+    retval = m->f(t, work, Jv, m->user_data);
+    m->nfeDQ++;
+    if (retval == 0) break;
+    if (retval < 0) return -1;
+    sig *= 0.25;
+  }
+  if (retval > 0) return 1;
+  const double siginv = 1.0 / sig;
+  v_linearsum(siginv, Jv, -siginv, fy, Jv);
+  return 0;
+}
+
 static int ls_atimes(void* mem, N_Vector v, N_Vector z)
 { /* cvLsATimes */
   CvlsPort* m = (CvlsPort*)mem;
-  int r       = m->jtimes(v, z, m->tn, m->ycur, m->fcur, m->user_data, m->ls_ytemp);
+  int r       = m->jtimes ? m->jtimes(v, z, m->tn, m->ycur, m->fcur, m->user_data, m->ls_ytemp)
+                          : dq_jtimes(m, v, z, m->tn, m->ycur, m->fcur, m->ls_ytemp);
   m->njtimes++;
   if (r != 0) return r;
   v_linearsum(1.0, v, -m->gamma, z, z);
@@ -355,7 +378,7 @@ static int newton_solve(CvlsPort* m, N_Vector ycor, double tol, int callLSetup)
       retval = nls_residual(m, ycor, delta);
       if (retval != 0) break;
     }
-    if ((retval > 0) && !m->nls_jcur)
+    if ((retval > 0) && !m->nls_jcur && m->pset)
     {
       m->nconvfails++;
       callLSetup = 1;
@@ -518,10 +541,15 @@ static void set_coeffs(CvlsPort* m)
 }
 
 static int nls(CvlsPort* m, int nflag)
-{ /* cvNls: lsetup exists (a preconditioner setup is attached) */
-  m->convfail   = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
-  int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (m->nst == 0) ||
-                  (m->nst >= m->nstlp + MSBP) || (fabs(m->gamrat - 1.0) > DGMAX_LSETUP);
+{ /* cvNls: CVLS has an lsetup only when a preconditioner setup is attached */
+  int callSetup = 0;
+  if (m->pset)
+  {
+    m->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
+    callSetup   = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (m->nst == 0) ||
+                (m->nst >= m->nstlp + MSBP) || (fabs(m->gamrat - 1.0) > DGMAX_LSETUP);
+  }
+  else m->crate = 1.0;
   v_const(0.0, m->acor);
   int flag = newton_solve(m, m->acor, m->tq[4], callSetup);
   m->nni += m->niters;
@@ -854,7 +882,9 @@ static int get_dky(CvlsPort* m, double t, N_Vector dky)
 
 /* CVodeCreate(CV_BDF) + CVodeInit(f, t0, y0) + CVodeSStolerances(rtol, atol)
  * + CVodeSetMaxNumSteps(mxstep) + CVodeSetLinearSolver(LS, NULL) +
- * CVodeSetJacTimes(NULL, jtimes) + CVodeSetPreconditioner(pset, psolve). */
+ * CVodeSetJacTimes(NULL, jtimes) (jtimes NULL: the difference quotient) +
+ * CVodeSetPreconditioner(pset, psolve) (pset may be NULL; psolve NULL: no
+ * preconditioner is attached). */
 void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double atol, long mxstep,
                        SUNLinearSolver LS, CvlsJTimesFn jtimes, CvlsPSetupFn pset,
                        CvlsPSolveFn psolve, void* user_data)
@@ -891,7 +921,8 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   m->eplifac   = CVLS_EPLIN;
   m->nrmfac    = sqrt((double)y0->ops->nvgetlength(y0));
   if (LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
-  if (LS->ops->setpreconditioner) LS->ops->setpreconditioner(LS, m, ls_psetup, ls_psolve);
+  if (LS->ops->setpreconditioner && psolve)
+    LS->ops->setpreconditioner(LS, m, pset ? ls_psetup : NULL, ls_psolve);
   return m;
 }
 
@@ -974,7 +1005,8 @@ int cvls_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 }
 
 /* Counters in CVodeGet* order: nst, nfe, nni, nnf, ncfn, netf, nsetups, nli,
- * npe, nps, njtimes, ncfl, qu, q (current); and hu, h (current), tn, h0u. */
+ * npe, nps, njtimes, ncfl, qu, q (current), nfeDQ (RHS evaluations of the
+ * difference-quotient J v); and hu, h (current), tn, h0u. */
 void cvls_port_stats(void* mem, long* c, double* r)
 {
   CvlsPort* m = (CvlsPort*)mem;
@@ -992,6 +1024,7 @@ void cvls_port_stats(void* mem, long* c, double* r)
   c[11] = m->ncfl;
   c[12] = m->qu;
   c[13] = m->next_q;
+  c[14] = m->nfeDQ;
   r[0]  = m->hu;
   r[1]  = m->next_h;
   r[2]  = m->tn;

@@ -29,7 +29,7 @@ from . import port
 
 REF_LIB = Path(__file__).resolve().parent / "_ref" / "libsundials_ref.so"
 COUNTER_NAMES = ("nst", "nfe", "nni", "nnf", "ncfn", "netf", "nsetups", "nli", "npe", "nps",
-                 "njtimes", "ncfl", "qu", "q")
+                 "njtimes", "ncfl", "qu", "q", "nfels")
 REAL_NAMES = ("hu", "h", "tn", "h0u")
 
 VP, D, I, I64 = ct.c_void_p, ct.c_double, ct.c_int, ct.c_int64
@@ -75,7 +75,7 @@ def ref_lib() -> ct.CDLL:
                  "CVodeGetNumNonlinSolvConvFails", "CVodeGetNumStepSolveFails",
                  "CVodeGetNumErrTestFails", "CVodeGetNumLinSolvSetups", "CVodeGetNumLinIters",
                  "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves", "CVodeGetNumJtimesEvals",
-                 "CVodeGetNumLinConvFails"):
+                 "CVodeGetNumLinConvFails", "CVodeGetNumLinRhsEvals"):
         f = getattr(L, name)
         f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
     for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
@@ -177,7 +177,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
     assert L.CVodeSetMaxNumSteps(mem, mxstep) == 0
     LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
     assert L.CVodeSetLinearSolver(mem, LS, None) == 0
-    assert L.CVodeSetJacTimes(mem, None, jt) == 0
+    if jt:
+        assert L.CVodeSetJacTimes(mem, None, jt) == 0
     assert L.CVodeSetPreconditioner(mem, ps, pv) == 0
     cnt, real, sols = [], [], []
     t = D()
@@ -196,6 +197,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
         for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
             getattr(L, name)(mem, ct.byref(li))
             row.append(li.value)
+        L.CVodeGetNumLinRhsEvals(mem, ct.byref(c))
+        row.append(c.value)
         rrow = []
         for name in ("CVodeGetLastStep", "CVodeGetCurrentStep", "CVodeGetCurrentTime",
                      "CVodeGetActualInitStep"):
@@ -230,7 +233,7 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
         P.cvls_port_set_vabstol(mem, rtol, vatol_handle)
     cnt, real, sols = [], [], []
     t = D()
-    c = (ct.c_long * 14)()
+    c = (ct.c_long * len(COUNTER_NAMES))()
     r = (D * 4)()
     try:
         for tout in touts:

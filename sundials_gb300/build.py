@@ -48,6 +48,7 @@ PER_FILE_FLAGS = {
     "sunlinsol_spgmr_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "heat2d_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "robertson_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "bruss3d_gb300.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

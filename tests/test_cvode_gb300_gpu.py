@@ -144,3 +144,64 @@ def test_cvode_robertson_mixed_block_preconditioner():
         yr = g["r1024_y"][j]
         w = float(np.sqrt(np.mean(((s[k] - yr) / (1e-4 * np.abs(yr) + atol)) ** 2)))
         assert w <= 1.0, (k, w)
+
+
+BR_GOLDEN = Path(__file__).resolve().parent / "golden" / "bruss3d_cvode_ref.npz"
+
+
+@pytest.mark.parametrize("shape,c", [((6, 5, 7), 0.01), ((6, 5, 7), -0.02), ((4, 4, 4), 0.0),
+                                     ((16, 16, 16), 0.01)])
+def test_bruss3d_functions_bit_identical(shape, c):
+    """Advection (both upwind directions and c = 0), reaction alone, the full
+    right-hand side and the per-cell reaction solve: bit for bit the
+    restatement of rhs3D.hpp."""
+    from oracle import bruss3d_cvode as bc
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    q = bc.Params(*shape, c=c)
+    rng = np.random.default_rng(7)
+    y = rng.uniform(0.5, 4.0, q.n)
+    b = rng.uniform(-1.0, 1.0, q.n)
+    Y, B, O = NVector.from_numpy(y), NVector.from_numpy(b), NVector(q.n)
+    P = Bruss3D(*shape, c=c)
+    try:
+        def beq(got, ref):
+            return np.array_equal(got.view(np.int64), ref.view(np.int64))
+        assert P.advection(Y, O) == 0 and beq(O.get(), bc.advection(q, y))
+        assert P.reaction(Y, O) == 0 and beq(O.get(), bc.reaction(q, y))
+        assert P.rhs(Y, O) == 0 and beq(O.get(), bc.rhs(q, y))
+        for gamma in (1e-6, 3.7e-3, 0.25):
+            assert P.solve_reaction(Y, O, B, gamma) == 0
+            assert beq(O.get(), bc.solve_reaction(q, y, b, gamma)), gamma
+        assert P.rhs(Y, Y) == -1  # the stencil needs distinct input and output
+    finally:
+        P.free()
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_cvode_bruss3d_matches_reference(fused, fma):
+    """The benchmark's CVODE configuration on a 16^3 grid to t = 10: the
+    reference's own reduction-order runs never moved a counter, so every
+    counter after every output must equal the reference's; the last
+    solution within 3x the reference's own weighted RMS deviation."""
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.spgmr import PREC_LEFT, SPGMR
+    g = np.load(BR_GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    assert S.set_fused(fused) == 0
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        c, r, s = hc.run_port(y.v, S.S, P.cvode_callbacks(), lambda h: y.get(),
+                              [float(t) for t in g["touts"]], rtol, atol)
+    finally:
+        S.free()
+        P.free()
+    assert np.array_equal(c, g["counters"]), (c[-1] - g["counters"][-1]).tolist()
+    yr = g["y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g["omp_wrms"].max()), 1e-6), w
