@@ -98,13 +98,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ distributed
-def dist_setup(n_gpus):
+# One process per GPU (torchrun); the batch is not split: every rank
+# integrates its own seeded batch (weak scaling, no data-path collective), and
+# only the timings meet, as the max over ranks.  The backend is NCCL on GPUs;
+# the same helpers run over gloo on CPU for the multi-process tests.
+_BACKEND = "nccl"
+
+
+def dist_setup(n_gpus, backend="nccl"):
+    global _BACKEND
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        _BACKEND = backend
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -114,24 +123,36 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(world, x):
+def _reduce(world, x, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if _BACKEND == "nccl" else "cpu")
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(world, x):
+    import torch.distributed as dist
+    return x if world == 1 else _reduce(world, x, dist.ReduceOp.MAX)
 
 
 def sum_over_ranks(world, x):
-    if world == 1:
-        return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return x if world == 1 else _reduce(world, x, dist.ReduceOp.SUM)
+
+
+def rank_seed(rank):
+    """Seed of rank's batch: rank 0 integrates the seed-1 batch the accuracy
+    checks use; the others get distinct seeds."""
+    return 1 if rank == 0 else 1 + rank * 1000003
+
+
+def weak_value(units_per_rank, steps, world, max_elapsed):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time."""
+    return units_per_rank * steps * world / max_elapsed
 
 
 # --------------------------------------------------------- nvector workload
@@ -416,7 +437,7 @@ def run_kinetics(args, world, rank, local):
     torch.cuda.set_device(local)
     # weak scaling: every rank integrates its own 65,536-system batch
     nsys = args.nsys
-    batch = K.generate(nsys, seed=1 + rank * 1000003 if rank else 1)
+    batch = K.generate(nsys, seed=rank_seed(rank))
     stats_bytes = K.BATCH_STATS_DTYPE.itemsize * nsys
     d_y0 = torch.from_numpy(batch.y0.copy()).cuda()
     d_yout = torch.zeros_like(d_y0)
@@ -436,7 +457,7 @@ def run_kinetics(args, world, rank, local):
     launches = (lib.SUNGB300_KernelLaunchCount() - l0) * args.steps // (args.steps + args.warmup)
     ck = clocks.stop(local) if rank == 0 else None
     elapsed = max_over_ranks(world, float(np.sum(times)))
-    value = nsys * args.steps * world / elapsed
+    value = weak_value(nsys, args.steps, world, elapsed)
     yout_mixed = d_yout.cpu().numpy()
     st = np.frombuffer(d_stats.cpu().numpy().tobytes(), K.BATCH_STATS_DTYPE)
 
@@ -448,7 +469,7 @@ def run_kinetics(args, world, rank, local):
     for _ in range(e2e_steps):
         y_host, st_host = B.solve(TOUT)
     e2e_el = max_over_ranks(world, time.perf_counter() - te)
-    e2e = nsys * e2e_steps * world / e2e_el
+    e2e = weak_value(nsys, e2e_steps, world, e2e_el)
 
     # ---- roofline of the integrator: FP64 work vs the live FP64 rate
     flops = float(np.sum(fp64_flops_per_system(st, batch.n, args.refine)))
@@ -459,7 +480,7 @@ def run_kinetics(args, world, rank, local):
     B64 = BatchBDF(batch).configure(RTOL, ATOL, "fp64")
     tune_fp64 = B64.autotune(stride=2)
     t64 = time_batch(B64, d_y0, d_yout, d_stats, max(1, args.steps // 2), 1, flush)
-    plain = nsys * world / max_over_ranks(world, float(np.mean(t64)))
+    plain = weak_value(nsys, 1, world, max_over_ranks(world, float(np.mean(t64))))
     yout_plain = d_yout.cpu().numpy()
 
     # ---- the N_Vector microbenchmark
