@@ -187,19 +187,17 @@ int SUNRoberts_GB300_CVPSetup(sunrealtype, N_Vector y, N_Vector, sunbooleantype 
 {
   SUNRoberts_GB300 p = (SUNRoberts_GB300)pv;
   if (!same_length(p, y) || !jcurPtr) return -1;
-  // the matrix lives on the legacy default stream; the vectors' work is
-  // ordered before it by the same stream or by this synchronisation
+  // the vectors' stream, on which the block LU (built on tmpl) works too
   cudaStream_t s = (cudaStream_t)N_VGetStream_GB300(y);
-  if (s) cudaStreamSynchronize(s);
   if (!jok)
   {
-    k_rob_jac<<<stream_grid(p->ncells), kBlock>>>(p->ncells, p->d_k,
-                                                  N_VGetDeviceArrayPointer_GB300(y), p->d_J);
+    k_rob_jac<<<stream_grid(p->ncells), kBlock, 0, s>>>(p->ncells, p->d_k,
+                                                        N_VGetDeviceArrayPointer_GB300(y), p->d_J);
     count_launch();
     *jcurPtr = SUNTRUE;
   }
   else *jcurPtr = SUNFALSE;
-  k_rob_newton_matrix<<<stream_grid(9 * p->ncells), kBlock>>>(
+  k_rob_newton_matrix<<<stream_grid(9 * p->ncells), kBlock, 0, s>>>(
     p->ncells, p->d_J, SUNMatrix_BlockDiag_GB300_Data(p->P), -gamma);
   count_launch();
   if (!check_cuda(cudaGetLastError(), "robertson psetup launch")) return -1;
