@@ -250,7 +250,62 @@ def nvector_measure(args, rank, local, steps, warmup):
     }
     for v in X + [Y, W, Z, Z2]:
         v.destroy()
+    out["sweep"] = nvector_sweep(rank)
     return out
+
+
+def nvector_sweep(rank, log2s=(20, 22, 24, 26)):
+    """The same five operations at 2^20 .. 2^26 elements, each timed over
+    back-to-back calls with CUDA events (no flush).  Where an operation's
+    operands fit in the 129 MB L2 (operands_fit_l2) the figure is L2
+    bandwidth or launch latency (and, for the reductions, the host read of
+    the result each call makes); from 2^24 every operation streams from HBM,
+    as at 2^28."""
+    import torch
+    from sundials_gb300 import _lib
+    from sundials_gb300.nvector import NVector
+
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    res = {}
+    for lg in log2s:
+        n = 1 << lg
+        xs, y, w, c5 = gen_inputs(n, seed=11 + rank)
+        X = [NVector.from_numpy(a, stream=sp) for a in xs]
+        W = NVector.from_numpy(w, stream=sp)
+        Z, Z2 = NVector(n, stream=sp), NVector(n, stream=sp)
+        ops = Z.ops
+        c5a = _lib.real_array(c5)
+        a5 = _lib.real_array(c5[::-1].copy() * 1e-3)
+        arrX = _lib.nv_array([v.v for v in X[:5]])
+        arrY = _lib.nv_array([v.v for v in X[1:6]])
+        dots = (ct.c_double * 5)()
+        calls = {
+            "LinearSum": lambda: ops["nvlinearsum"](0.3, X[0].v, 0.7, X[1].v, Z.v),
+            "LinearCombination5": lambda: ops["nvlinearcombination"](5, c5a, arrX, Z2.v),
+            "DotProdMulti5": lambda: ops["nvdotprodmulti"](5, X[5].v, arrX, dots),
+            "WrmsNorm": lambda: ops["nvwrmsnorm"](X[0].v, W.v),
+            "ScaleAddMulti5": lambda: ops["nvscaleaddmulti"](5, a5, X[0].v, arrY, arrY),
+        }
+        reps = max(10, min(400, (1 << 30) // (n * 48)))
+        row = {}
+        for name, fn in calls.items():
+            for _ in range(3):
+                fn()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            us = e0.elapsed_time(e1) * 1e3 / reps
+            row[name] = {"us": round(us, 2), "GBs": round(NV_BYTES[name] * n / (us * 1e-6) / 1e9, 1),
+                         "operands_fit_l2": NV_BYTES[name] * n < 129e6}
+        res["2^%d" % lg] = row
+        for v in X + [W, Z, Z2]:
+            v.destroy()
+    return res
 
 
 def spgmr_measure(nx=2048, solves=20, warmup=3):
