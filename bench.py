@@ -258,9 +258,10 @@ def nvector_sweep(rank, log2s=(20, 22, 24, 26)):
     """The same five operations at 2^20 .. 2^26 elements, each timed over
     back-to-back calls with CUDA events (no flush).  Where an operation's
     operands fit in the 129 MB L2 (operands_fit_l2) the figure is L2
-    bandwidth or launch latency (and, for the reductions, the host read of
-    the result each call makes); from 2^24 every operation streams from HBM,
-    as at 2^28."""
+    bandwidth or launch latency; the reductions (DotProdMulti, WrmsNorm)
+    return their result to the host on every call, so at small sizes their
+    figure is that round trip plus this Python caller's overhead.  From 2^24
+    every operation streams from HBM, as at 2^28."""
     import torch
     from sundials_gb300 import _lib
     from sundials_gb300.nvector import NVector
