@@ -17,6 +17,9 @@ namespace bdf {
 cudaError_t launch_fast(const Params& P, int mode, int nb, int grid, cudaStream_t stream,
                         const int32_t* order, int64_t count, unsigned int* next);
 cudaError_t occupancy_fast(int mode, int nb, int* per_sm);
+cudaError_t launch_fast_learn(const Params& P, int mode, int nb, int grid, cudaStream_t stream,
+                              const int32_t* order, int64_t count, unsigned int* next);
+cudaError_t occupancy_fast_learn(int mode, int nb, int* per_sm);
 cudaError_t launch_exact(const Params& P, int nb, int grid, cudaStream_t stream,
                          const int32_t* order, int64_t count, unsigned int* next);
 cudaError_t occupancy_exact(int nb, int* per_sm);
@@ -62,6 +65,7 @@ struct SUNBatchBDF_GB300_
   // retry of failed systems (fast modes): mode of the retry launch, or -1
   int retry_mode   = -2;  // the other fast mode
   int per_sm[3][3] = {};   // [mode][width class] resident warps per SM
+  int per_sm_learn[3][3] = {};  // the same for the kernels with the learned predictor
   int plan_id[3]   = {0, 0, 1};  // launch plan per mode (index into kPlanWidths)
   std::vector<int32_t> h_order;   // systems by decreasing n (host copy, for sampling)
 
@@ -112,13 +116,25 @@ bool query_occupancy(SUNBatchBDF_GB300 b)
                                                        : occupancy_fast(mode, widths[k], &per_sm);
       if (!gb300::check_cuda(e, "k_batch_bdf occupancy")) return false;
       b->per_sm[mode][k] = per_sm < 1 ? 1 : per_sm;
+      if (mode != SUNBATCHBDF_FP64_EXACT)
+      {
+        int pl = 0;
+        if (!gb300::check_cuda(occupancy_fast_learn(mode, widths[k], &pl),
+                               "k_batch_bdf occupancy"))
+          return false;
+        b->per_sm_learn[mode][k] = pl < 1 ? 1 : pl;
+      }
     }
   return true;
 }
 
+// the predictor or the recorder is attached: the LEARN kernels run
+inline bool uses_learn(const Params& P) { return P.mlp_w != nullptr || P.rec_x != nullptr; }
+
 int grid_for(SUNBatchBDF_GB300 b, int mode, int nb, int64_t need)
 {
-  int grid = gb300::num_sms() * b->per_sm[mode][width_index(nb)];
+  const bool learn = mode != SUNBATCHBDF_FP64_EXACT && (b->mlp_w || b->rec_x);
+  int grid = gb300::num_sms() * (learn ? b->per_sm_learn : b->per_sm)[mode][width_index(nb)];
   if (need < grid) grid = (int)need;
   return grid < 1 ? 1 : grid;
 }
@@ -436,8 +452,10 @@ cudaError_t launch_plan(SUNBatchBDF_GB300 b, const Params& P, const Launch* L, i
     e = (b->mode == SUNBATCHBDF_FP64_EXACT)
           ? launch_exact(P, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
                          b->d_next + L[k].queue)
-          : launch_fast(P, b->mode, L[k].nb, L[k].grid, b->stream, L[k].order, L[k].count,
-                        b->d_next + L[k].queue);
+          : uses_learn(P) ? launch_fast_learn(P, b->mode, L[k].nb, L[k].grid, b->stream,
+                                              L[k].order, L[k].count, b->d_next + L[k].queue)
+                          : launch_fast(P, b->mode, L[k].nb, L[k].grid, b->stream, L[k].order,
+                                        L[k].count, b->d_next + L[k].queue);
     gb300::count_launch();
   }
   return e;

@@ -232,7 +232,10 @@ __device__ __forceinline__ double cv_root(double x, int k)
   return EXACT ? dd_pow(x, inv_int(k)) : fast_root(x, k);
 }
 
-template <int MODE, int NB>
+// LEARN: the learned-predictor inference, its features and the training-data
+// recorder are compiled in; the default kernels leave that code out (it is
+// cold there, but its size costs instruction-cache misses in the hot loop).
+template <int MODE, int NB, bool LEARN = false>
 struct Integrator
 {
   static constexpr bool EXACT = (MODE == SUNBATCHBDF_FP64_EXACT);
@@ -928,7 +931,7 @@ struct Integrator
     if (dcon <= 1.0)
     {
       // ||ycor|| = ||delta|| after one iteration only when Newton started from 0
-      acnrm = (mcur == 0 && !learned_start) ? del : wrms(ycor);
+      acnrm = (mcur == 0 && !(LEARN && learned_start)) ? del : wrms(ycor);
       rv    = R_SUCCESS;
     }
     else if ((mcur >= 1) && (del > RDIV * delp)) rv = R_CONV_RECVR;
@@ -1260,9 +1263,9 @@ struct Integrator
     bool have_res = false;
     learned_start = false;
     float xr[5];
-    const bool learn = !EXACT && (P.mlp_w != nullptr || P.rec_x != nullptr);
+    const bool learn = LEARN && !EXACT && (P.mlp_w != nullptr || P.rec_x != nullptr);
     if (learn) mlp_features(xr);
-    if (!EXACT && P.mlp_w)
+    if (LEARN && !EXACT && P.mlp_w)
     {
       // learned initial iterate; kept only if its residual is the smaller
       float o0, o1;
@@ -1289,7 +1292,7 @@ struct Integrator
     }
     int flag = newton_solve(w.acor, tq[4], callSetup, have_res);
     if (flag != R_SUCCESS) return flag;
-    if (!EXACT && P.rec_x)
+    if (LEARN && !EXACT && P.rec_x)
     {
       // training pair: features and the converged corrector in error-weight units
       unsigned long long idx = 0;
@@ -1753,7 +1756,7 @@ struct Integrator
 // its size bucket (n <= NB) from the bucket's queue until the queue is empty
 // (no waiting on other warps or blocks).  Dynamic shared memory holds the
 // warp's vectors and its Newton matrix.
-template <int MODE, int NB>
+template <int MODE, int NB, bool LEARN = false>
 __global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
   k_batch_bdf(Params P, const int32_t* order, int64_t count, unsigned int* next)
 {
@@ -1765,7 +1768,7 @@ __global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
   int* pivbuf      = P.pivots + (size_t)slot * NMAX;
   WarpMem<NB>* mem = (WarpMem<NB>*)smem;
   void* mat        = L::mat_in_smem ? (void*)(smem + L::mem_bytes) : (void*)(scratch + SLOT_J);
-  Integrator<MODE, NB> I(P, *mem, mat, lane);
+  Integrator<MODE, NB, LEARN> I(P, *mem, mat, lane);
   if (P.count_dev)
   {  // a retry launch: its queue length was produced on the device
     const int64_t c = (int64_t)*P.count_dev;
@@ -1783,6 +1786,55 @@ __global__ void __launch_bounds__(32, Layout<MODE, NB>::min_blocks)
   if (lane == 0 && P.timers)
     for (int t = 0; t < T_COUNT; t++) P.timers[(size_t)slot * T_COUNT + t] += I.tacc[t];
 #endif
+}
+
+// Host-side launch and occupancy of the fast modes' kernels (FP64, MIXED);
+// each translation unit instantiates one LEARN variant.  The kernel's
+// shared-memory limit is set by fast_occupancy at creation.
+template <int MODE, int NB, bool LEARN>
+cudaError_t fast_launch_one(const Params& P, int grid, cudaStream_t stream, const int32_t* order,
+                            int64_t count, unsigned int* next)
+{
+  const size_t smem = Layout<MODE, NB>::warp_bytes;
+  k_batch_bdf<MODE, NB, LEARN><<<grid, 32, smem, stream>>>(P, order, count, next);
+  return cudaGetLastError();
+}
+
+template <int MODE, int NB, bool LEARN>
+cudaError_t fast_occ_one(int* per_sm)
+{
+  const size_t smem = Layout<MODE, NB>::warp_bytes;
+  cudaFuncSetAttribute(k_batch_bdf<MODE, NB, LEARN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_batch_bdf<MODE, NB, LEARN>, 32,
+                                                       smem);
+}
+
+template <bool LEARN>
+cudaError_t fast_launch(const Params& P, int mode, int nb, int grid, cudaStream_t stream,
+                        const int32_t* order, int64_t count, unsigned int* next)
+{
+  constexpr int M = SUNBATCHBDF_MIXED, F = SUNBATCHBDF_FP64;
+  if (mode == M)
+    return nb <= 32   ? fast_launch_one<M, 32, LEARN>(P, grid, stream, order, count, next)
+           : nb <= 48 ? fast_launch_one<M, 48, LEARN>(P, grid, stream, order, count, next)
+                      : fast_launch_one<M, 64, LEARN>(P, grid, stream, order, count, next);
+  return nb <= 32   ? fast_launch_one<F, 32, LEARN>(P, grid, stream, order, count, next)
+         : nb <= 48 ? fast_launch_one<F, 48, LEARN>(P, grid, stream, order, count, next)
+                    : fast_launch_one<F, 64, LEARN>(P, grid, stream, order, count, next);
+}
+
+template <bool LEARN>
+cudaError_t fast_occupancy(int mode, int nb, int* per_sm)
+{
+  constexpr int M = SUNBATCHBDF_MIXED, F = SUNBATCHBDF_FP64;
+  if (mode == M)
+    return nb <= 32   ? fast_occ_one<M, 32, LEARN>(per_sm)
+           : nb <= 48 ? fast_occ_one<M, 48, LEARN>(per_sm)
+                      : fast_occ_one<M, 64, LEARN>(per_sm);
+  return nb <= 32   ? fast_occ_one<F, 32, LEARN>(per_sm)
+         : nb <= 48 ? fast_occ_one<F, 48, LEARN>(per_sm)
+                    : fast_occ_one<F, 64, LEARN>(per_sm);
 }
 
 }  // namespace bdf
