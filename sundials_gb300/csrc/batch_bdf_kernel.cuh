@@ -246,7 +246,10 @@ struct Integrator
   const int lane;
   // system
   int n, nr;
-  bool two;      // n > 32: lanes own a second element
+  bool two;      // n > 32: lanes own a second element (read it through has2())
+  // a compile-time false in the 32-wide kernels, so their second-element
+  // code is not generated at all
+  __device__ __forceinline__ bool has2() const { return NB > 32 && two; }
   double inv_n;  // 1/n (fast modes)
   double* rdiag; // reciprocal pivots of the factorisation (fast modes)
   const int32_t *rt, *ra, *rb, *rc, *fptr, *fent, *jptr, *jent;
@@ -286,7 +289,7 @@ struct Integrator
     double s;
     if (EXACT)
     {
-      for (int i = lane; i < n; i += 32)
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
       {
         double p = x[i] * w.ewt[i];
         w.red[i] = p * p;
@@ -299,7 +302,7 @@ struct Integrator
     else
     {
       double acc = 0.0;
-      for (int i = lane; i < n; i += 32)
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
       {
         double p = x[i] * w.ewt[i];
         acc      = fma(p, p, acc);
@@ -312,7 +315,7 @@ struct Integrator
 
   __device__ void set_ewt(const double* ycur, double* wt)
   {  // cvEwtSetSS (cvode.c:4791)
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double t   = fabs(ycur[i]);
       t          = P.rtol * t;
@@ -334,7 +337,7 @@ struct Integrator
       w.rate[r] = v;
     }
     __syncwarp();
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double acc = 0.0;
       for (int e = fptr[i]; e < fptr[i + 1]; e++)
@@ -356,7 +359,7 @@ struct Integrator
     BDF_TIC(t0);
     for (int e = lane; e < n * n; e += 32) J[e] = 0.0;
     __syncwarp();
-    for (int j = lane; j < n; j += 32)
+    for (int j = lane; j < n && (NB > 32 || j < 32); j += 32)
     {
       double* col = J + j * n;
       for (int e = jptr[j]; e < jptr[j + 1]; e++)
@@ -423,7 +426,7 @@ struct Integrator
       if (lane == 0) piv[k] = l;
       if (bk == 0) return k + 1;
       if (l != k)
-        for (int j = lane; j < n; j += 32)
+        for (int j = lane; j < n && (NB > 32 || j < 32); j += 32)
         {
           T t           = a[j * ld + l];
           a[j * ld + l] = a[j * ld + k];
@@ -488,7 +491,7 @@ struct Integrator
     const int nq   = lr >> 2;
     float4* A4     = reinterpret_cast<float4*>(a);
     const int i0   = lane, i1 = lane + 32;
-    const bool h0  = i0 < n, h1 = two && i1 < n;
+    const bool h0  = i0 < n, h1 = has2() && i1 < n;
     for (int k = 0; k < n; k++)
     {
       long long bk = -1;
@@ -624,7 +627,7 @@ struct Integrator
     const int nq      = lr >> 2;
     const float4* A4  = reinterpret_cast<const float4*>(A);
     const float4* B4  = reinterpret_cast<const float4*>(w.fcol);
-    const bool h0 = lane < n, h1 = two && lane + 32 < n;
+    const bool h0 = lane < n, h1 = has2() && lane + 32 < n;
     float4 s0 = make_float4(0.f, 0.f, 0.f, 0.f), s1 = s0;
     for (int c = 0; c < nq; c++)
     {
@@ -665,7 +668,7 @@ struct Integrator
       {
         xj[u] = __shfl_sync(0xffffffffu, (j + u) < 32 ? x0 : x1, (j + u) & 31);
         v0[u] = lane < n ? J[(j + u) * n + lane] : 0.0;
-        v1[u] = (two && lane + 32 < n) ? J[(j + u) * n + lane + 32] : 0.0;
+        v1[u] = (has2() && lane + 32 < n) ? J[(j + u) * n + lane + 32] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 8; u += 2)
@@ -673,7 +676,7 @@ struct Integrator
         a0 = fma(v0[u], xj[u], a0);
         c0 = fma(v0[u + 1], xj[u + 1], c0);
       }
-      if (two)
+      if (has2())
 #pragma unroll
         for (int u = 0; u < 8; u += 2)
         {
@@ -685,7 +688,7 @@ struct Integrator
     {
       const double xj = __shfl_sync(0xffffffffu, j < 32 ? x0 : x1, j & 31);
       if (lane < n) a0 = fma(J[j * n + lane], xj, a0);
-      if (two && lane + 32 < n) a1 = fma(J[j * n + lane + 32], xj, a1);
+      if (has2() && lane + 32 < n) a1 = fma(J[j * n + lane + 32], xj, a1);
     }
     y0 = a0 + c0;
     y1 = a1 + c1;
@@ -713,7 +716,7 @@ struct Integrator
       const T bk  = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
       const T* ck = a + k * ld;
       if (lane > k && lane < n) b0 -= ck[lane] * bk;
-      if (two && lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
+      if (has2() && lane + 32 > k && lane + 32 < n) b1 -= ck[lane + 32] * bk;
     }
     for (int k = n - 1; k > 0; k--)
     {
@@ -734,7 +737,7 @@ struct Integrator
       }
       const T bk = __shfl_sync(0xffffffffu, k < 32 ? b0 : b1, k & 31);
       if (lane < k) b0 -= ck[lane] * bk;
-      if (two && lane + 32 < k) b1 -= ck[lane + 32] * bk;
+      if (has2() && lane + 32 < k) b1 -= ck[lane + 32] * bk;
     }
     if (lane == 0)
     {
@@ -791,7 +794,7 @@ struct Integrator
         M[j * ld + i] = J[e] * c;
       }
       __syncwarp();
-      for (int i = lane; i < n; i += 32) M[i * ld + i] += 1.0;
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) M[i * ld + i] += 1.0;
       __syncwarp();
       lu = getrf<double>(M);
     }
@@ -856,10 +859,10 @@ struct Integrator
   // cvNlsResidual (cvode_nls.c:363)
   __device__ void nls_residual(const double* ycor, double* res)
   {
-    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + ycor[i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.y[i] = w.zn[0][i] + ycor[i];
     rhs(w.y, w.ftemp);
     const double a = -gamma;
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double r = (rl1 * w.zn[1][i]) + ycor[i];
       res[i]   = r + a * w.ftemp[i];
@@ -869,10 +872,10 @@ struct Integrator
   // the same residual at ycor = 0 (the BDF predictor itself)
   __device__ void nls_residual0(double* res)
   {
-    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + 0.0;
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.y[i] = w.zn[0][i] + 0.0;
     rhs(w.y, w.ftemp);
     const double a = -gamma;
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double r = (rl1 * w.zn[1][i]) + 0.0;
       res[i]   = r + a * w.ftemp[i];
@@ -963,10 +966,10 @@ struct Integrator
       for (;;)
       {
         niters++;
-        for (int i = lane; i < n; i += 32) w.delta[i] = -w.delta[i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.delta[i] = -w.delta[i];
         __syncwarp();
         nls_lsolve(w.delta);
-        for (int i = lane; i < n; i += 32) ycor[i] = ycor[i] + w.delta[i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) ycor[i] = ycor[i] + w.delta[i];
         retval = nls_convtest(ycor, tol, curiter);
         curiter++;
         if (retval == R_SUCCESS)
@@ -990,7 +993,7 @@ struct Integrator
         callLSetup    = 1;
         jbad          = 1;
         learned_start = false;
-        for (int i = lane; i < n; i += 32) ycor[i] = 0.0;
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) ycor[i] = 0.0;
         continue;
       }
       break;
@@ -1007,7 +1010,7 @@ struct Integrator
     double c = eta;
     for (int j = 1; j <= q; j++)
     {
-      for (int i = lane; i < n; i += 32) w.zn[j][i] *= c;
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j][i] *= c;
       c = eta * c;
     }
     h      = hscale * eta;
@@ -1035,10 +1038,10 @@ struct Integrator
         xiold = xi;
       }
     A1 = (-alpha0 - alpha1) / prod;
-    for (int i = lane; i < n; i += 32) w.zn[L][i] = A1 * w.zn[indx_acor][i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[L][i] = A1 * w.zn[indx_acor][i];
     if (q > 1)
       for (int j = 2; j <= q; j++)
-        for (int i = lane; i < n; i += 32) w.zn[j][i] += l[j] * w.zn[L][i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j][i] += l[j] * w.zn[L][i];
   }
 
   __device__ void decrease_bdf()
@@ -1057,7 +1060,7 @@ struct Integrator
       for (int j = 2; j < q; j++)
       {
         const double c = -l[j];
-        for (int i = lane; i < n; i += 32) w.zn[j][i] += c * w.zn[q][i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j][i] += c * w.zn[q][i];
       }
   }
 
@@ -1085,7 +1088,7 @@ struct Integrator
     tn += h;
     for (int k = 1; k <= q; k++)
       for (int j = q; j >= k; j--)
-        for (int i = lane; i < n; i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] + w.zn[j][i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] + w.zn[j][i];
   }
 
   __device__ void restore(double saved_t)
@@ -1093,7 +1096,7 @@ struct Integrator
     tn = saved_t;
     for (int k = 1; k <= q; k++)
       for (int j = q; j >= k; j--)
-        for (int i = lane; i < n; i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] - w.zn[j][i];
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j - 1][i] = w.zn[j - 1][i] - w.zn[j][i];
   }
 
   __device__ void set_tq_bdf(double hsum, double alpha0, double alpha0_hat, double xi_inv,
@@ -1259,7 +1262,7 @@ struct Integrator
     convfail      = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
     int callSetup = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (nst == 0) ||
                     (nst >= nstlp + MSBP) || (fabs(gamrat - 1.0) > DGMAX_LSETUP);
-    for (int i = lane; i < n; i += 32) w.acor[i] = 0.0;
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.acor[i] = 0.0;
     bool have_res = false;
     learned_start = false;
     float xr[5];
@@ -1282,7 +1285,7 @@ struct Integrator
       learned_start = rl < r0;
       if (learned_start) nlpu++;
       else
-        for (int i = lane; i < n; i += 32)
+        for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
         {
           w.acor[i]  = 0.0;
           w.delta[i] = w.tempv[i];
@@ -1310,7 +1313,7 @@ struct Integrator
           rtg[i] = i < n ? (float)(w.acor[i] * w.ewt[i]) : 0.0f;
       }
     }
-    for (int i = lane; i < n; i += 32) w.y[i] = w.zn[0][i] + w.acor[i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.y[i] = w.zn[0][i] + w.acor[i];
     cv_jcur = 0;
     return R_SUCCESS;
   }
@@ -1366,7 +1369,7 @@ struct Integrator
     qwait  = LONG_WAIT;
     nscon  = 0;
     rhs(w.zn[0], w.tempv);
-    for (int i = lane; i < n; i += 32) w.zn[1][i] = h * w.tempv[i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[1][i] = h * w.tempv[i];
     return TRY_AGAIN;
   }
 
@@ -1382,12 +1385,12 @@ struct Integrator
     for (int j = 0; j <= q; j++)
     {
       const double c = l[j];
-      for (int i = lane; i < n; i += 32) w.zn[j][i] += c * w.acor[i];
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[j][i] += c * w.acor[i];
     }
     qwait--;
     if ((qwait == 1) && (q != QMAX))
     {
-      for (int i = lane; i < n; i += 32) w.zn[QMAX][i] = w.acor[i];
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[QMAX][i] = w.acor[i];
       saved_tq5 = tq[5];
       indx_acor = QMAX;
     }
@@ -1438,7 +1441,7 @@ struct Integrator
       for (int i = 1; i <= L; i++) p *= base;  // SUNRpowerI
       double cquot   = (tq[5] / saved_tq5) * p;
       const double a = -cquot;
-      for (int i = lane; i < n; i += 32) w.tempv[i] = (a * w.zn[QMAX][i]) + w.acor[i];
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.tempv[i] = (a * w.zn[QMAX][i]) + w.acor[i];
       double dup = wrms(w.tempv) * tq[3];
       etaqp1     = 1.0 / (cv_root<EXACT>(BIAS3 * dup, L + 1) + ADDON);
     }
@@ -1467,7 +1470,7 @@ struct Integrator
     {
       eta    = etaqp1;
       qprime = q + 1;
-      for (int i = lane; i < n; i += 32) w.zn[QMAX][i] = w.acor[i];
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[QMAX][i] = w.acor[i];
     }
   }
 
@@ -1523,7 +1526,7 @@ struct Integrator
     prepare_next_step(dsm);
     BDF_TOC(t0, T_PREP);
     etamax = (nst <= SMALL_NST) ? ETA_MAX_ES : ETA_MAX_GS;
-    for (int i = lane; i < n; i += 32) w.acor[i] *= tq[2];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.acor[i] *= tq[2];
     return CV_SUCCESS;
   }
 
@@ -1533,9 +1536,9 @@ struct Integrator
     double* temp1 = w.tempv;
     double* temp2 = w.acor;
     double loc    = 0.0;
-    for (int i = lane; i < n; i += 32) temp2[i] = fabs(w.zn[0][i]);
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) temp2[i] = fabs(w.zn[0][i]);
     set_ewt(w.zn[0], temp1);
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double t1 = 1.0 / temp1[i];
       t1        = t1 + HUB_FACTOR * temp2[i];
@@ -1552,11 +1555,11 @@ struct Integrator
 
   __device__ double ydd_norm(double hg)
   {  // cvYddNorm (cvode.c:2323)
-    for (int i = lane; i < n; i += 32) w.y[i] = (hg * w.zn[1][i]) + w.zn[0][i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.y[i] = (hg * w.zn[1][i]) + w.zn[0][i];
     rhs(w.y, w.tempv);
     const double a = 1.0 / hg, b = -1.0 / hg;
     const bool sdiff = (a == -b) && (a != 1.0) && (a != -1.0);
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
       w.tempv[i] = sdiff ? a * (w.tempv[i] - w.zn[1][i]) : (a * w.tempv[i]) + (b * w.zn[1][i]);
     return wrms(w.tempv);
   }
@@ -1610,7 +1613,7 @@ struct Integrator
       js[nvec] = j;
       nvec++;
     }
-    for (int i = lane; i < n; i += 32)
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32)
     {
       double v;
       if (nvec == 2) v = (c[0] * w.zn[js[0]][i]) + (c[1] * w.zn[js[1]][i]);
@@ -1649,7 +1652,7 @@ struct Integrator
     inv_n = 1.0 / n;
 
     const double* y0 = P.y0 + p.y_off[s];
-    for (int i = lane; i < n; i += 32) w.zn[0][i] = y0[i];
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[0][i] = y0[i];
     tn = P.t0;
     h = hscale = hprime = next_h = eta = etaq = etaqm1 = etaqp1 = hu = h0u = 0.0;
     next_q = 0;
@@ -1676,7 +1679,7 @@ struct Integrator
     hscale = h;
     hprime = h;
     h0u    = h;
-    for (int i = lane; i < n; i += 32) w.zn[1][i] *= h;
+    for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) w.zn[1][i] *= h;
 
     long nstloc = 0;
     BDF_TIC(tall);
@@ -1720,7 +1723,7 @@ struct Integrator
     double* yo = P.yout + p.y_off[s];
     if (istate == CV_SUCCESS) get_dky(tout, yo);
     else
-      for (int i = lane; i < n; i += 32) yo[i] = w.zn[0][i];
+      for (int i = lane; i < n && (NB > 32 || i < 32); i += 32) yo[i] = w.zn[0][i];
     if (lane == 0 && P.stats)
     {
       SUNBatchBDFStats st;
