@@ -63,8 +63,9 @@ int main(void) {
 
 
 def test_abi_header_matches_reference_headers(tmp_path):
-    """Compile the same layout probe against this build's header alone and
-    against the reference's own headers (when present): identical output."""
+    """Compile the same layout probe against include/sundials_gb300_abi.h
+    alone and against the reference's own headers (when present): identical
+    output."""
     src = tmp_path / "layout.c"
     src.write_text(_layout_program(None, None))
     out_own = tmp_path / "own"
