@@ -44,6 +44,12 @@ SUNGB300_EXPORT int SUNRoberts_GB300_RHS(sunrealtype t, N_Vector y, N_Vector ydo
 /* CVLsJacTimesVecFn: Jv = J(y) v */
 SUNGB300_EXPORT int SUNRoberts_GB300_JTimes(N_Vector v, N_Vector Jv, sunrealtype t, N_Vector y,
                                             N_Vector fy, void* p, N_Vector tmp);
+/* CVLsJacFn: J(y) into a SUNMatrix_BlockDiag_GB300 of ncells 3x3 blocks, for
+ * CVodeSetLinearSolver(cvode_mem, SUNLinSol_BlockLU_GB300(y, J, ...), J) +
+ * CVodeSetJacFn -- the reference example's direct block solve
+ * (cvRoberts_block_cusolversp_batchqr.cu:196-223, there on cuSolverSp). */
+SUNGB300_EXPORT int SUNRoberts_GB300_Jac(sunrealtype t, N_Vector y, N_Vector fy, SUNMatrix J,
+                                         void* p, N_Vector tmp1, N_Vector tmp2, N_Vector tmp3);
 /* CVLsPrecSetupFn / CVLsPrecSolveFn: exact block-Jacobi preconditioner.
  * Setup returns 1 (recoverable) if a block is singular. */
 SUNGB300_EXPORT int SUNRoberts_GB300_CVPSetup(sunrealtype t, N_Vector y, N_Vector fy,

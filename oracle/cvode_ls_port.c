@@ -1,7 +1,9 @@
 /* cvode_ls_port.c -- TEST ORACLE (checker only, never part of the product).
  *
- * CVODE with BDF, the Newton nonlinear solver and a matrix-free iterative
- * SUNLinearSolver (user Jacobian-times-vector and preconditioner), restated
+ * CVODE with BDF, the Newton nonlinear solver and either a matrix-free
+ * iterative SUNLinearSolver (user or difference-quotient Jacobian-times-
+ * vector, optional preconditioner) or a matrix-based direct one (SUNMatrix,
+ * user Jacobian), restated
  * over the generic object model: every vector operation is dispatched through
  * the vector's ops table the way the reference's generic layer dispatches it
  * (fused and vector-array operations when the vector provides them, the
@@ -21,7 +23,7 @@
  *   CVodeGetDky (k = 0)            cvode.c:1671-1750
  *   cvNlsResidual / LSetup / LSolve / ConvTest   src/cvode/cvode_nls.c:256-398
  *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-330
- *   CVodeSetLinearSolver defaults for a matrix-free iterative solver,
+ *   CVodeSetLinearSolver defaults, cvLsInitialize (saved J), cvLsLinSys,
  *   cvLsATimes / cvLsDQJtimes / cvLsPSetup / cvLsPSolve, cvLsSetup, cvLsSolve
  *                                  src/cvode/cvode_ls.c:56-285, 895-980, 1536-1900
  *   N_VLinearCombination / N_VScaleAddMulti / N_VScaleVectorArray dispatch
@@ -87,6 +89,8 @@ typedef int (*CvlsPSetupFn)(double t, N_Vector y, N_Vector fy, sunbooleantype jo
                             sunbooleantype* jcurPtr, double gamma, void* user_data);
 typedef int (*CvlsPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
                             double gamma, double delta, int lr, void* user_data);
+typedef int (*CvlsJacFn)(double t, N_Vector y, N_Vector fy, SUNMatrix J, void* user_data,
+                         N_Vector tmp1, N_Vector tmp2, N_Vector tmp3);
 
 typedef struct
 {
@@ -99,14 +103,17 @@ typedef struct
   double rtol, atol;
   long mxstep;
   SUNLinearSolver LS;
+  SUNMatrix A, savedJ; /* matrix-based (direct) solver: A and CVLS's saved J */
+  CvlsJacFn jac;
   /* vectors */
   N_Vector zn[QMAX + 1], ewt, acor, tempv, ftemp, y, delta, ls_x, ls_ytemp;
+  N_Vector vtemp1, vtemp2, vtemp3;
   N_Vector ycur, fcur; /* CVLS's pointers to the current state and RHS */
   N_Vector Vabstol;    /* CVodeSVtolerances' copy, or NULL for scalar atol */
   /* CVLS */
   double nrmfac, eplifac;
   sunbooleantype jbad;
-  long nstlj, npe, nli, nps, ncfl, njtimes, nfeDQ;
+  long nstlj, npe, nli, nps, ncfl, njtimes, nfeDQ, nje;
   int initialized;
   /* Newton */
   int curiter;
@@ -223,7 +230,28 @@ static int ls_psolve(void* mem, N_Vector r, N_Vector z, double tol, int lr)
   return ret;
 }
 
-/* cvLsSetup, matrix-free: jcurPtr is &cv_jcur */
+/* cvLsLinSys (cvode_ls.c:1311-1400): A = I - gamma J with J new or saved */
+static int ls_linsys(CvlsPort* m, N_Vector ypred, N_Vector fpred)
+{
+  if (!m->jbad)
+  {
+    m->cv_jcur = SUNFALSE;
+    if (m->savedJ->ops->copy(m->savedJ, m->A)) return -1;
+  }
+  else
+  {
+    m->cv_jcur = SUNTRUE;
+    if (m->LS->ops->gettype(m->LS) == SUNLINEARSOLVER_DIRECT && m->A->ops->zero(m->A)) return -1;
+    int retval = m->jac(m->tn, ypred, fpred, m->A, m->user_data, m->vtemp1, m->vtemp2, m->vtemp3);
+    if (retval < 0) return -1;
+    if (retval > 0) return 1;
+    if (m->A->ops->copy(m->A, m->savedJ)) return -1;
+  }
+  if (m->A->ops->scaleaddi(-m->gamma, m->A)) return -1;
+  return 0;
+}
+
+/* cvLsSetup (cvode_ls.c:1536-1640); jcurPtr is &cv_jcur */
 static int ls_setup(CvlsPort* m, int convfail, N_Vector ypred, N_Vector fpred)
 {
   m->ycur       = ypred;
@@ -231,6 +259,17 @@ static int ls_setup(CvlsPort* m, int convfail, N_Vector ypred, N_Vector fpred)
   double dgamma = fabs((m->gamma / m->gammap) - 1.0);
   m->jbad       = (m->nst == 0) || (m->nst >= m->nstlj + CVLS_MSBJ) ||
             ((convfail == FAIL_BAD_J) && (dgamma < CVLS_DGMAX)) || (convfail == FAIL_OTHER);
+  if (m->A)
+  { /* matrix-based */
+    int retval = ls_linsys(m, ypred, fpred);
+    if (m->cv_jcur)
+    {
+      m->nje++;
+      m->nstlj = m->nst;
+    }
+    if (retval != 0) return retval;
+    return m->LS->ops->setup(m->LS, m->A);
+  }
   m->cv_jcur = m->jbad;
   int flag   = m->LS->ops->setup(m->LS, NULL);
   if (m->cv_jcur)
@@ -247,6 +286,30 @@ static int ls_setup(CvlsPort* m, int convfail, N_Vector ypred, N_Vector fpred)
 static int ls_solve(CvlsPort* m, N_Vector b, N_Vector weight, N_Vector ynow, N_Vector fnow)
 {
   const int curiter = m->curiter;
+  if (m->A)
+  { /* direct: no tolerance, x = A^{-1} b, BDF solution scaling (scalesol) */
+    m->ycur = ynow;
+    m->fcur = fnow;
+    if (m->LS->ops->setscalingvectors) m->LS->ops->setscalingvectors(m->LS, weight, weight);
+    v_const(0.0, m->ls_x);
+    if (m->LS->ops->setzeroguess) m->LS->ops->setzeroguess(m->LS, SUNTRUE);
+    int retval = m->LS->ops->solve(m->LS, m->A, m->ls_x, b, 0.0);
+    v_scale(1.0, m->ls_x, b);
+    if (m->gamrat != 1.0) v_scale(2.0 / (1.0 + m->gamrat), b, b);
+    if (retval != 0) m->ncfl++;
+    switch (retval)
+    {
+    case 0: return 0;
+    case SUNLS_RES_REDUCED: return curiter == 0 ? 0 : 1;
+    case SUNLS_CONV_FAIL:
+    case SUNLS_ATIMES_FAIL_REC:
+    case SUNLS_PSOLVE_FAIL_REC:
+    case SUNLS_PACKAGE_FAIL_REC:
+    case SUNLS_QRFACT_FAIL:
+    case SUNLS_LUFACT_FAIL: return 1;
+    default: return retval < 0 ? -1 : 0;
+    }
+  }
   double deltar     = m->eplifac * m->tq[4];
   double bnorm      = v_wrms(b, weight);
   if (bnorm <= deltar)
@@ -378,7 +441,7 @@ static int newton_solve(CvlsPort* m, N_Vector ycor, double tol, int callLSetup)
       retval = nls_residual(m, ycor, delta);
       if (retval != 0) break;
     }
-    if ((retval > 0) && !m->nls_jcur && m->pset)
+    if ((retval > 0) && !m->nls_jcur && (m->pset || m->A))
     {
       m->nconvfails++;
       callLSetup = 1;
@@ -543,7 +606,7 @@ static void set_coeffs(CvlsPort* m)
 static int nls(CvlsPort* m, int nflag)
 { /* cvNls: CVLS has an lsetup only when a preconditioner setup is attached */
   int callSetup = 0;
-  if (m->pset)
+  if (m->pset || m->A)
   {
     m->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
     callSetup   = (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) || (m->nst == 0) ||
@@ -901,6 +964,9 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   m->delta    = clone(y0);
   m->ls_ytemp = clone(y0);
   m->ls_x     = clone(y0);
+  m->vtemp1   = clone(y0);
+  m->vtemp2   = clone(y0);
+  m->vtemp3   = clone(y0);
   v_scale(1.0, y0, m->zn[0]);
   m->f         = f;
   m->jtimes    = jtimes;
@@ -926,6 +992,16 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   return m;
 }
 
+/* CVodeSetLinearSolver(LS, A) with a matrix and a direct solver, and
+ * CVodeSetJacFn(jac): the matrix-based path of CVLS (create the object with
+ * LS and no J v / preconditioner, then attach A and jac). */
+void cvls_port_set_matrix(void* mem, SUNMatrix A, CvlsJacFn jac)
+{
+  CvlsPort* m = (CvlsPort*)mem;
+  m->A        = A;
+  m->jac      = jac;
+}
+
 /* CVodeSVtolerances(rtol, abstol): a copy of abstol is kept (all entries > 0). */
 void cvls_port_set_vabstol(void* mem, double rtol, N_Vector abstol)
 {
@@ -943,8 +1019,9 @@ int cvls_port_solve(void* mem, double tout, N_Vector yout, double* tret)
   if (m->nst == 0)
   {
     if (!m->initialized)
-    { /* cvInitialSetup: ewt, then cvLsInitialize */
+    { /* cvInitialSetup: ewt, then cvLsInitialize (the saved J of a matrix) */
       set_ewt(m, m->zn[0], m->ewt);
+      if (m->A && !m->savedJ) m->savedJ = m->A->ops->clone(m->A);
       m->LS->ops->initialize(m->LS);
       m->initialized = 1;
     }
@@ -1006,7 +1083,7 @@ int cvls_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 
 /* Counters in CVodeGet* order: nst, nfe, nni, nnf, ncfn, netf, nsetups, nli,
  * npe, nps, njtimes, ncfl, qu, q (current), nfeDQ (RHS evaluations of the
- * difference-quotient J v); and hu, h (current), tn, h0u. */
+ * difference-quotient J v), nje; and hu, h (current), tn, h0u. */
 void cvls_port_stats(void* mem, long* c, double* r)
 {
   CvlsPort* m = (CvlsPort*)mem;
@@ -1025,6 +1102,7 @@ void cvls_port_stats(void* mem, long* c, double* r)
   c[12] = m->qu;
   c[13] = m->next_q;
   c[14] = m->nfeDQ;
+  c[15] = m->nje;
   r[0]  = m->hu;
   r[1]  = m->next_h;
   r[2]  = m->tn;
@@ -1035,9 +1113,11 @@ void cvls_port_free(void* mem)
 {
   CvlsPort* m = (CvlsPort*)mem;
   if (!m) return;
-  N_Vector vs[] = {m->ewt, m->acor, m->tempv, m->ftemp, m->y, m->delta, m->ls_ytemp, m->ls_x};
+  N_Vector vs[] = {m->ewt,   m->acor, m->tempv,  m->ftemp,  m->y,     m->delta,
+                   m->ls_ytemp, m->ls_x, m->vtemp1, m->vtemp2, m->vtemp3};
   for (int i = 0; i < (int)(sizeof(vs) / sizeof(vs[0])); i++) vs[i]->ops->nvdestroy(vs[i]);
   for (int j = 0; j <= QMAX; j++) m->zn[j]->ops->nvdestroy(m->zn[j]);
   if (m->Vabstol) m->Vabstol->ops->nvdestroy(m->Vabstol);
+  if (m->savedJ) m->savedJ->ops->destroy(m->savedJ);
   free(m);
 }

@@ -29,7 +29,7 @@ from . import port
 
 REF_LIB = Path(__file__).resolve().parent / "_ref" / "libsundials_ref.so"
 COUNTER_NAMES = ("nst", "nfe", "nni", "nnf", "ncfn", "netf", "nsetups", "nli", "npe", "nps",
-                 "njtimes", "ncfl", "qu", "q", "nfels")
+                 "njtimes", "ncfl", "qu", "q", "nfels", "nje")
 REAL_NAMES = ("hu", "h", "tn", "h0u")
 
 VP, D, I, I64 = ct.c_void_p, ct.c_double, ct.c_int, ct.c_int64
@@ -37,6 +37,7 @@ RHS_FN = ct.CFUNCTYPE(I, D, VP, VP, VP)
 JTIMES_FN = ct.CFUNCTYPE(I, VP, VP, D, VP, VP, VP, VP)
 PSETUP_FN = ct.CFUNCTYPE(I, D, VP, VP, I, ct.POINTER(I), D, VP)
 PSOLVE_FN = ct.CFUNCTYPE(I, D, VP, VP, VP, VP, D, D, I, VP)
+JAC_FN = ct.CFUNCTYPE(I, D, VP, VP, VP, VP, VP, VP, VP)
 
 
 def initial(nx: int, ny: int, seed: int = 1) -> np.ndarray:
@@ -57,6 +58,11 @@ def ref_lib() -> ct.CDLL:
         ("N_VDestroy", None, [VP]),
         ("N_VGetArrayPointer", ct.POINTER(D), [VP]),
         ("SUNLinSol_SPGMR", VP, [VP, I, I, VP]),
+        ("SUNDenseMatrix", VP, [I64, I64, VP]),
+        ("SUNDenseMatrix_Data", ct.POINTER(D), [VP]),
+        ("SUNMatDestroy", None, [VP]),
+        ("SUNLinSol_Dense", VP, [VP, VP, VP]),
+        ("CVodeSetJacFn", I, [VP, VP]),
         ("SUNLinSolFree", I, [VP]),
         ("CVodeCreate", VP, [I, VP]),
         ("CVodeInit", I, [VP, VP, D, VP]),
@@ -75,7 +81,7 @@ def ref_lib() -> ct.CDLL:
                  "CVodeGetNumNonlinSolvConvFails", "CVodeGetNumStepSolveFails",
                  "CVodeGetNumErrTestFails", "CVodeGetNumLinSolvSetups", "CVodeGetNumLinIters",
                  "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves", "CVodeGetNumJtimesEvals",
-                 "CVodeGetNumLinConvFails", "CVodeGetNumLinRhsEvals"):
+                 "CVodeGetNumLinConvFails", "CVodeGetNumLinRhsEvals", "CVodeGetNumJacEvals"):
         f = getattr(L, name)
         f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
     for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
@@ -101,6 +107,8 @@ def port_lib() -> ct.CDLL:
         L.cvls_port_free.argtypes = [VP]
         L.cvls_port_set_vabstol.restype = None
         L.cvls_port_set_vabstol.argtypes = [VP, D, VP]
+        L.cvls_port_set_matrix.restype = None
+        L.cvls_port_set_matrix.argtypes = [VP, VP, VP]
         L._cvls_declared = True
     return L
 
@@ -151,12 +159,15 @@ def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
     return c, r, s, u0
 
 
-def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, threads=None):
+def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, threads=None,
+                       direct=False):
     """The reference's CVode (BDF, Newton, SPGMR with left preconditioning and
     maxl 5, user J v and preconditioner) on the problem whose serial
     callbacks make_serial(L) builds (an object with .addresses() -> (f,
     jtimes, psetup, psolve) and .arr(N_Vector) -> numpy view).  atol: a
-    scalar (CVodeSStolerances) or an array (CVodeSVtolerances)."""
+    scalar (CVodeSStolerances) or an array (CVodeSVtolerances).  direct:
+    SUNDenseMatrix + SUNLINSOL_DENSE and the problem's .jac_address() instead
+    (the matrix-based path of CVLS)."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -175,11 +186,18 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
         prob.arr(vatol)[:] = atol
         assert L.CVodeSVtolerances(mem, rtol, vatol) == 0
     assert L.CVodeSetMaxNumSteps(mem, mxstep) == 0
-    LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
-    assert L.CVodeSetLinearSolver(mem, LS, None) == 0
-    if jt:
-        assert L.CVodeSetJacTimes(mem, None, jt) == 0
-    assert L.CVodeSetPreconditioner(mem, ps, pv) == 0
+    A = None
+    if direct:
+        A = L.SUNDenseMatrix(n, n, ctx)
+        LS = L.SUNLinSol_Dense(y, A, ctx)
+        assert L.CVodeSetLinearSolver(mem, LS, A) == 0
+        assert L.CVodeSetJacFn(mem, prob.jac_address()) == 0
+    else:
+        LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+        assert L.CVodeSetLinearSolver(mem, LS, None) == 0
+        if jt:
+            assert L.CVodeSetJacTimes(mem, None, jt) == 0
+        assert L.CVodeSetPreconditioner(mem, ps, pv) == 0
     cnt, real, sols = [], [], []
     t = D()
     for tout in touts:
@@ -199,6 +217,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
             row.append(li.value)
         L.CVodeGetNumLinRhsEvals(mem, ct.byref(c))
         row.append(c.value)
+        L.CVodeGetNumJacEvals(mem, ct.byref(c))
+        row.append(c.value)
         rrow = []
         for name in ("CVodeGetLastStep", "CVodeGetCurrentStep", "CVodeGetCurrentTime",
                      "CVodeGetActualInitStep"):
@@ -210,6 +230,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
     pm = VP(mem)
     L.CVodeFree(ct.byref(pm))
     L.SUNLinSolFree(LS)
+    if A:
+        L.SUNMatDestroy(A)
     L.N_VDestroy(y)
     if vatol:
         L.N_VDestroy(vatol)
@@ -218,12 +240,14 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
-             vatol_handle=None):
+             vatol_handle=None, matrix=None):
     """The restated CVODE on whatever objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (f, jtimes, psetup, psolve,
     user_data) addresses, get(handle) -> numpy copy of a vector;
-    vatol_handle: an N_Vector of absolute tolerances (else atol, a scalar)."""
+    vatol_handle: an N_Vector of absolute tolerances (else atol, a scalar);
+    matrix = (SUNMatrix, CVLsJacFn address): the matrix-based path with a
+    direct LS_handle (callbacks then only need f and the user data)."""
     P = port_lib()
     f, jt, ps, pv, data = callbacks
     mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, 0.0 if vatol_handle else atol, mxstep,
@@ -231,6 +255,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
     assert mem
     if vatol_handle:
         P.cvls_port_set_vabstol(mem, rtol, vatol_handle)
+    if matrix is not None:
+        P.cvls_port_set_matrix(mem, matrix[0], matrix[1])
     cnt, real, sols = [], [], []
     t = D()
     c = (ct.c_long * len(COUNTER_NAMES))()
@@ -254,23 +280,34 @@ def run_port_serial(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10):
                                 atol)
 
 
-def run_port_serial_with(make_serial, u0, touts, rtol, atol):
+def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False):
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
     prob = make_serial(L)
-    y = L.N_VNew_Serial(len(u0), ctx)
+    n = len(u0)
+    y = L.N_VNew_Serial(n, ctx)
     prob.arr(y)[:] = u0
-    LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+    A, matrix = None, None
+    if direct:
+        A = L.SUNDenseMatrix(n, n, ctx)
+        LS = L.SUNLinSol_Dense(y, A, ctx)
+        matrix = (A, prob.jac_address())
+        cbs = (prob.addresses()[0], None, None, None, None)
+    else:
+        LS = L.SUNLinSol_SPGMR(y, 1, 5, ctx)
+        cbs = prob.addresses() + (None,)
     vatol = None
     if np.ndim(atol) != 0:
-        vatol = L.N_VNew_Serial(len(u0), ctx)
+        vatol = L.N_VNew_Serial(n, ctx)
         prob.arr(vatol)[:] = atol
     try:
-        return run_port(y, LS, prob.addresses() + (None,), lambda h: prob.arr(h).copy(), touts,
-                        rtol, atol, vatol_handle=vatol)
+        return run_port(y, LS, cbs, lambda h: prob.arr(h).copy(), touts, rtol, atol,
+                        vatol_handle=vatol, matrix=matrix)
     finally:
         L.SUNLinSolFree(LS)
+        if A:
+            L.SUNMatDestroy(A)
         L.N_VDestroy(y)
         if vatol:
             L.N_VDestroy(vatol)

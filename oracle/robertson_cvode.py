@@ -172,22 +172,50 @@ class SerialRobertson:
             arr(z)[:] = getrs(self.P, self.piv, arr(r))
             return 0
 
+        nc = len(k)
+        cell = np.arange(nc)
+
+        def jac_dense(t, y, fy, J, data, t1, t2, t3):
+            # SUNDenseMatrix (column-major, zeroed by CVODE): the 3x3 blocks
+            D = np.ctypeslib.as_array(L.SUNDenseMatrix_Data(J), shape=(self.n, self.n))
+            Jb = jac(self.k, arr(y))
+            for col in range(3):
+                for row in range(3):
+                    D[3 * cell + col, 3 * cell + row] = Jb[:, col, row]
+            return 0
+
         self.cbs = (hc.RHS_FN(f), hc.JTIMES_FN(jt), hc.PSETUP_FN(psetup), hc.PSOLVE_FN(psolve))
+        self.jac_cb = hc.JAC_FN(jac_dense)
         self.arr = arr
 
     def addresses(self):
         return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs)
 
+    def jac_address(self):
+        return hc.ct.cast(self.jac_cb, hc.VP).value
+
 
 def run_reference(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, threads=None):
+    """SPGMR with the exact block-Jacobi preconditioner."""
     k = rates(ncells)
     atol = vector_atol(ncells) if atol is None else atol
     return hc.run_reference_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
                                  atol, threads=threads)
 
 
-def run_port_serial(ncells: int, touts=TOUTS, rtol=1e-4, atol=None):
+def run_port_serial(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, direct=False):
     k = rates(ncells)
     atol = vector_atol(ncells) if atol is None else atol
     return hc.run_port_serial_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
-                                   atol)
+                                   atol, direct=direct)
+
+
+def run_reference_direct(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, threads=None):
+    """The reference example's configuration (cvRoberts_block_cusolversp_batchqr.cu:
+    a direct solver on the block-diagonal Newton matrix with the user Jacobian),
+    on the reference's CPU objects: SUNDenseMatrix + SUNLINSOL_DENSE, whose
+    partial-pivoting LU of a block-diagonal matrix is the per-block LU."""
+    k = rates(ncells)
+    atol = vector_atol(ncells) if atol is None else atol
+    return hc.run_reference_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
+                                 atol, threads=threads, direct=True)

@@ -182,6 +182,21 @@ int SUNRoberts_GB300_JTimes(N_Vector v, N_Vector Jv, sunrealtype, N_Vector y, N_
   return check_cuda(cudaGetLastError(), "robertson jtimes launch") ? 0 : -1;
 }
 
+int SUNRoberts_GB300_Jac(sunrealtype, N_Vector y, N_Vector, SUNMatrix J, void* pv, N_Vector,
+                         N_Vector, N_Vector)
+{
+  SUNRoberts_GB300 p = (SUNRoberts_GB300)pv;
+  if (!same_length(p, y) || !J || SUNMatrix_BlockDiag_GB300_Rows(J) != 3 * p->ncells ||
+      SUNMatrix_BlockDiag_GB300_NNZ(J) != 9 * p->ncells)
+    return -1;
+  cudaStream_t s = (cudaStream_t)N_VGetStream_GB300(y);
+  k_rob_jac<<<stream_grid(p->ncells), kBlock, 0, s>>>(p->ncells, p->d_k,
+                                                      N_VGetDeviceArrayPointer_GB300(y),
+                                                      SUNMatrix_BlockDiag_GB300_Data(J));
+  count_launch();
+  return check_cuda(cudaGetLastError(), "robertson jac launch") ? 0 : -1;
+}
+
 int SUNRoberts_GB300_CVPSetup(sunrealtype, N_Vector y, N_Vector, sunbooleantype jok,
                               sunbooleantype* jcurPtr, sunrealtype gamma, void* pv)
 {

@@ -44,6 +44,10 @@ class Robertson:
         return (addr("SUNRoberts_GB300_RHS"), addr("SUNRoberts_GB300_JTimes"),
                 addr("SUNRoberts_GB300_CVPSetup"), addr("SUNRoberts_GB300_CVPSolve"), self.p)
 
+    def jac_address(self) -> int:
+        """CVLsJacFn filling a SUNMatrix_BlockDiag_GB300 of 3x3 blocks."""
+        return ct.cast(self.lib.SUNRoberts_GB300_Jac, ct.c_void_p).value
+
     def free(self) -> None:
         if self.p:
             self.lib.SUNRoberts_GB300_Free(self.p)

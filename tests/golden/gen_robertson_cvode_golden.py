@@ -5,7 +5,10 @@ problem of oracle/robertson_cvode.py (cells with k = (0.04, 3e7, 1e4) x
 exp(0.1 z), y0 = (1, 0, 0), rtol 1e-4 and the per-species absolute
 tolerances 1e-8 / 1e-14 / 1e-6 of cvRoberts_block_cusolversp_batchqr.cu,
 outputs 0.4 * 10^k for k = 0..11; SPGMR with left preconditioning, maxl 5,
-the user J v and the exact block-Jacobi preconditioner of cvDiurnal_kry.c).
+the user J v and the exact block-Jacobi preconditioner of cvDiurnal_kry.c;
+the rd* cases: the example's own configuration, a direct solver on the
+block-diagonal Newton matrix with the user Jacobian -- SUNDenseMatrix +
+SUNLINSOL_DENSE on the CPU).
 Per case: the rate constants, the counters after each output, hu / h / tn /
 h0u, the solutions at the outputs listed in <case>_y_index, and the same runs on NVECTOR_OPENMP with 2, 3, 4, 6, 8 and 16 threads (a
 sample of the reference's own sensitivity to the summation order of its
@@ -27,16 +30,18 @@ from oracle import robertson_cvode as rc  # noqa: E402
 
 OUT = Path(__file__).resolve().parent / "robertson_cvode_ref.npz"
 THREADS = (2, 3, 4, 6, 8, 16)
-# name: (cells, outputs whose solutions are stored)
-CASES = {"r256": (256, list(range(12))), "r1024": (1024, [5, 11])}
+# name: (cells, outputs whose solutions are stored, direct solver)
+CASES = {"r256": (256, list(range(12)), False), "r1024": (1024, [5, 11], False),
+         "rd256": (256, list(range(12)), True), "rd1024": (1024, [5, 11], True)}
 RTOL = 1e-4
 
 
 def main():
     out = {}
-    for name, (ncells, keep) in CASES.items():
+    for name, (ncells, keep, direct) in CASES.items():
         atol = rc.vector_atol(ncells)
-        c, r, s = rc.run_reference(ncells, rc.TOUTS, RTOL, atol)
+        run = rc.run_reference_direct if direct else rc.run_reference
+        c, r, s = run(ncells, rc.TOUTS, RTOL, atol)
         out[f"{name}_k"] = rc.rates(ncells)
         out[f"{name}_touts"] = np.array(rc.TOUTS)
         out[f"{name}_rtol"] = np.array(RTOL)
@@ -47,7 +52,7 @@ def main():
         print(name, dict(zip(hc.COUNTER_NAMES, c[-1].tolist())))
         oc, ow = [], []
         for th in THREADS:
-            c2, _, s2 = rc.run_reference(ncells, rc.TOUTS, RTOL, atol, threads=th)
+            c2, _, s2 = run(ncells, rc.TOUTS, RTOL, atol, threads=th)
             w = 1.0 / (RTOL * np.abs(s) + atol)
             oc.append(c2[-1])
             ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))

@@ -32,10 +32,9 @@ def test_golden_fixture_layout():
         assert g[f"{name}_y"].shape == (len(touts), nx * ny)
         assert g[f"{name}_u0"].shape == (nx * ny,)
         assert np.all(g[f"{name}_counters"][:, 0] > 0)
-        # the reference's own summation-order sample: steps never move
+        # the reference's own summation-order sample
         oc = g[f"{name}_omp_counters"]
         assert oc.shape == (len(g[f"{name}_omp_threads"]), len(hc.COUNTER_NAMES))
-        assert np.all(oc[:, 0] == g[f"{name}_counters"][-1, 0])
 
 
 @needs_ref
