@@ -25,6 +25,9 @@
 //    nvector_cuda.cu:1527).
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <atomic>
+#include <chrono>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -209,6 +212,41 @@ inline bool sync_stream(N_Vector v)
 }
 
 inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// Reduction results reach the host through pinned, mapped memory written by
+// the kernel's last block.  Before a launch the host marks the m result slots
+// with a signalling-NaN pattern that no arithmetic produces; after it, the
+// host polls them until every slot holds a result, which skips the stream
+// synchronisation's round trip on the common path.  A reduction still
+// running after 2 ms (long vectors) or a failed launch falls back to
+// cudaStreamSynchronize, which waits for completion and reports errors.
+constexpr uint64_t kResultPending = 0x7ff4dead5eed0001ull;
+
+inline void arm_results(double* h_result, int m)
+{
+  volatile uint64_t* r = (volatile uint64_t*)h_result;
+  for (int j = 0; j < m; ++j) r[j] = kResultPending;
+  std::atomic_thread_fence(std::memory_order_seq_cst);
+}
+
+inline bool wait_results(N_Vector v, const double* h_result, int m)
+{
+  const volatile uint64_t* r = (const volatile uint64_t*)h_result;
+  const auto t0              = std::chrono::steady_clock::now();
+  for (unsigned it = 1;; ++it)
+  {
+    bool done = true;
+    for (int j = 0; j < m && done; ++j) done = r[j] != kResultPending;
+    if (done)
+    {
+      std::atomic_thread_fence(std::memory_order_acquire);
+      return true;
+    }
+    if ((it & 1023u) == 0 &&
+        std::chrono::steady_clock::now() - t0 > std::chrono::milliseconds(2))
+      return sync_stream(v);
+  }
+}
 
 // ============================================================ device kernels
 
@@ -887,11 +925,12 @@ double launch_reduce(N_Vector ref, int64_t n, const double* a, const double* b,
             (E::NIN < 3 || aligned16(c)) && (!E::WRITES || aligned16(z));
   int64_t items = vec ? (n + 1) / 2 : n;
   int grid      = reduce_grid(items);
+  arm_results(ws->h_result, 1);
   k_reduce<Op, E><<<grid, kBlock, 0, ws->stream>>>(n, a, b, c, z, e, vec, ws->d_partials,
                                                    ws->d_counter, ws->d_result);
   count_launch();
   if (!ok_or_report(ref, cudaGetLastError(), "k_reduce launch")) return NAN;
-  if (!sync_stream(ref)) return NAN;
+  if (!wait_results(ref, ws->h_result, 1)) return NAN;
   return ws->h_result[0];
 }
 
@@ -1067,6 +1106,7 @@ bool dotmulti_core(int nvec, N_Vector x, N_Vector* Y, double* out)
     }
     int64_t items = vec ? (n + 1) / 2 : n;
     int grid      = reduce_grid(items);
+    arm_results(ws->h_result, m);
     switch (m)
     {
     case 1: launch_dotmulti<1>(x, args, vec, grid); break;
@@ -1080,7 +1120,7 @@ bool dotmulti_core(int nvec, N_Vector x, N_Vector* Y, double* out)
     }
     count_launch();
     if (!ok_or_report(x, cudaGetLastError(), "k_dotmulti launch")) return false;
-    if (!sync_stream(x)) return false;
+    if (!wait_results(x, ws->h_result, m)) return false;
     for (int j = 0; j < m; ++j) out[k0 + j] = ws->h_result[j];
   }
   return true;
@@ -1152,6 +1192,7 @@ bool va_wsqr(int nvec, N_Vector* X, N_Vector* W, N_Vector id, double* out)
     int64_t items = vec ? (n + 1) / 2 : n;
     dim3 grid(reduce_grid(items), m);
     const double* idp = id ? D(id) : nullptr;
+    arm_results(ws->h_result, m);
     if (id)
       DISPATCH_F(ref,
                  (k_va_wsqr<true, true><<<grid, kBlock, 0, ws->stream>>>(
@@ -1166,7 +1207,7 @@ bool va_wsqr(int nvec, N_Vector* X, N_Vector* W, N_Vector id, double* out)
                    n, args, idp, vec, ws->d_partials, ws->d_counter, ws->d_result)));
     count_launch();
     if (!ok_or_report(ref, cudaGetLastError(), "k_va_wsqr launch")) return false;
-    if (!sync_stream(ref)) return false;
+    if (!wait_results(ref, ws->h_result, m)) return false;
     for (int j = 0; j < m; ++j) out[r0 + j] = ws->h_result[j];
   }
   return true;
