@@ -254,13 +254,14 @@ def nvector_measure(args, rank, local, steps, warmup):
     return out
 
 
-def nvector_sweep(rank, log2s=(20, 22, 24, 26)):
-    """The same five operations at 2^20 .. 2^26 elements, each timed over
+def nvector_sweep(rank, log2s=(12, 16, 20, 22, 24, 26)):
+    """The same five operations at 2^12 .. 2^26 elements, each timed over
     back-to-back calls with CUDA events (no flush).  Where an operation's
     operands fit in the 129 MB L2 (operands_fit_l2) the figure is L2
     bandwidth or launch latency; the reductions (DotProdMulti, WrmsNorm)
     return their result to the host on every call, so at small sizes their
-    figure is that round trip plus this Python caller's overhead.  From 2^24
+    figure is that round trip (the "us" per call; the Python caller adds
+    ~0.25 us).  From 2^24
     every operation streams from HBM, as at 2^28."""
     import torch
     from sundials_gb300 import _lib

@@ -41,9 +41,13 @@ inline int stream_grid(int64_t items)
 }
 
 // Reductions: enough blocks to fill the GPU, each block reading at least 4
-// element pairs per thread; the launch shape depends only on the length.
+// element pairs per thread; up to 8,192 pairs one block does it all (its
+// result is written directly: no last-block ticket, no fence, no second
+// block to schedule -- latency is all that counts at that size).  The launch
+// shape depends only on the length.
 inline int reduce_grid(int64_t items)
 {
+  if (items <= 8192) return 1;
   int64_t need = (items + 4 * kBlock - 1) / (4 * kBlock);
   int64_t cap  = (int64_t)num_sms() * 4;
   if (cap > kMaxRedBlocks) cap = kMaxRedBlocks;
