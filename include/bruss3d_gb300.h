@@ -49,7 +49,9 @@ SUNGB300_EXPORT int SUNBruss3D_GB300_RHS(sunrealtype t, N_Vector y, N_Vector ydo
 /* x = (I - gamma dg/dy)^{-1} b per cell, at the state y. */
 SUNGB300_EXPORT int SUNBruss3D_GB300_SolveReaction(N_Vector y, N_Vector x, N_Vector b,
                                                    sunrealtype gamma, void* p);
-/* CVLsPrecSolveFn: z = (I - gamma dg/dy)^{-1} r (the benchmark's PSolve). */
+/* CVLsPrecSolveFn / ARKLsPrecSolveFn (same signature): z = (I - gamma
+ * dg/dy)^{-1} r, the benchmark's PSolve for its CVODE and ARK-DIRK drivers
+ * (cvode_driver.cpp:96-102, arkode_driver.cpp:117-130). */
 SUNGB300_EXPORT int SUNBruss3D_GB300_CVPSolve(sunrealtype t, N_Vector y, N_Vector fy,
                                               N_Vector r, N_Vector z, sunrealtype gamma,
                                               sunrealtype delta, int lr, void* p);

@@ -1,0 +1,215 @@
+"""TEST ORACLE (checker only): ARKStep DIRK runs (implicit right-hand side
+only, Newton, SPGMR with left preconditioning and the default maxl, the
+difference-quotient J v, a preconditioner solve without setup) -- the
+ARK-DIRK configuration of the 3-D advection-reaction benchmark
+(benchmarks/advection_reaction_3D/raja/arkode_driver.cpp:51-160, default
+order 3) -- by two drivers:
+
+* ``run_reference_with``: the reference's own ARKodeEvolve on its
+  NVECTOR_SERIAL / SUNLINSOL_SPGMR objects (``oracle/_ref``), which also
+  returns the Butcher table the run used (ARKStepGetCurrentButcherTables);
+* ``run_port``: the C restatement ``oracle/arkode_dirk_port.c`` on whatever
+  N_Vector and SUNLinearSolver it is given, with that table as an input.
+
+Both return the counters after every output time (COUNTER_NAMES), the step
+sizes and times (REAL_NAMES) and the solutions there."""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import heat_cvode as hc
+from . import port
+
+COUNTER_NAMES = ("nst", "nst_attempts", "nfi", "netf", "ncfn", "nni", "nnf", "nli", "nps",
+                 "njtimes", "nfeDQ", "ncfl")
+REAL_NAMES = ("hold", "hnext", "tcur", "h0u")
+TABLE_KEYS = ("A", "b", "c", "d", "orders")
+
+VP, D, I, I64 = hc.VP, hc.D, hc.I, hc.I64
+
+
+class _Table(ct.Structure):
+    """struct ARKodeButcherTableMem (include/arkode/arkode_butcher.h:33-42)."""
+    _fields_ = [("q", I), ("p", I), ("stages", I), ("A", ct.POINTER(ct.POINTER(D))),
+                ("c", ct.POINTER(D)), ("b", ct.POINTER(D)), ("d", ct.POINTER(D))]
+
+
+def ref_lib() -> ct.CDLL:
+    L = hc.ref_lib()
+    if getattr(L, "_ark_declared", False):
+        return L
+    for name, res, args in [
+        ("ARKStepCreate", VP, [VP, VP, D, VP, VP]),
+        ("ARKodeSetOrder", I, [VP, I]),
+        ("ARKodeSStolerances", I, [VP, D, D]),
+        ("ARKodeSetMaxNumSteps", I, [VP, ct.c_long]),
+        ("SUNNonlinSol_Newton", VP, [VP, VP]),
+        ("SUNNonlinSolFree", I, [VP]),
+        ("ARKodeSetNonlinearSolver", I, [VP, VP]),
+        ("ARKodeSetLinearSolver", I, [VP, VP, VP]),
+        ("ARKodeSetPreconditioner", I, [VP, VP, VP]),
+        ("ARKodeEvolve", I, [VP, D, VP, ct.POINTER(D), I]),
+        ("ARKodeFree", None, [ct.POINTER(VP)]),
+        ("ARKStepGetCurrentButcherTables", I, [VP, ct.POINTER(ct.POINTER(_Table)),
+                                               ct.POINTER(ct.POINTER(_Table))]),
+        ("ARKodeGetNumRhsEvals", I, [VP, I, ct.POINTER(ct.c_long)]),
+    ]:
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
+    for name in ("ARKodeGetNumSteps", "ARKodeGetNumStepAttempts", "ARKodeGetNumErrTestFails",
+                 "ARKodeGetNumStepSolveFails", "ARKodeGetNumNonlinSolvIters",
+                 "ARKodeGetNumNonlinSolvConvFails", "ARKodeGetNumLinIters",
+                 "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals", "ARKodeGetNumLinRhsEvals",
+                 "ARKodeGetNumLinConvFails"):
+        f = getattr(L, name)
+        f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
+    for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
+                 "ARKodeGetActualInitStep"):
+        f = getattr(L, name)
+        f.restype, f.argtypes = I, [VP, ct.POINTER(D)]
+    L._ark_declared = True
+    return L
+
+
+def port_lib() -> ct.CDLL:
+    L = port.lib()
+    if not getattr(L, "_arkdirk_declared", False):
+        DP = ct.POINTER(D)
+        L.arkdirk_port_create.restype = VP
+        L.arkdirk_port_create.argtypes = [VP, D, VP, D, D, ct.c_long, VP, VP, VP, VP, I, I, I,
+                                          DP, DP, DP, DP]
+        L.arkdirk_port_solve.restype = I
+        L.arkdirk_port_solve.argtypes = [VP, D, VP, ct.POINTER(D)]
+        L.arkdirk_port_stats.restype = None
+        L.arkdirk_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
+        L.arkdirk_port_free.restype = None
+        L.arkdirk_port_free.argtypes = [VP]
+        L._arkdirk_declared = True
+    return L
+
+
+def _read_table(T: _Table) -> dict:
+    s = T.stages
+    A = np.array([[T.A[i][j] for j in range(s)] for i in range(s)])
+    return {"A": A, "b": np.array([T.b[i] for i in range(s)]),
+            "c": np.array([T.c[i] for i in range(s)]),
+            "d": np.array([T.d[i] for i in range(s)]), "orders": np.array([T.q, T.p])}
+
+
+def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None):
+    """The reference's ARKodeEvolve on the problem whose serial callbacks
+    make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
+    psetup None, and .arr(N_Vector)): (counters, reals, solutions, table).
+    threads = k: NVECTOR_OPENMP on k threads instead of NVECTOR_SERIAL (its
+    reductions sum in another order)."""
+    L = ref_lib()
+    ctx = VP()
+    assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
+    prob = make_serial(L)
+    n = len(u0)
+    y = L.N_VNew_Serial(n, ctx) if threads is None else L.N_VNew_OpenMP(n, threads, ctx)
+    prob.arr(y)[:] = u0
+    f, jt, ps, pv = prob.addresses()
+    assert ps is None and jt is None
+    mem = L.ARKStepCreate(None, f, 0.0, y, ctx)
+    assert mem
+    assert L.ARKodeSetOrder(mem, order) == 0
+    assert L.ARKodeSStolerances(mem, rtol, atol) == 0
+    assert L.ARKodeSetMaxNumSteps(mem, mxstep) == 0
+    NLS = L.SUNNonlinSol_Newton(y, ctx)
+    assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
+    LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    assert L.ARKodeSetLinearSolver(mem, LS, None) == 0
+    assert L.ARKodeSetPreconditioner(mem, None, pv) == 0
+    cnt, real, sols = [], [], []
+    t, c, r = D(), ct.c_long(), D()
+    table = None
+    for tout in touts:
+        flag = L.ARKodeEvolve(mem, tout, y, ct.byref(t), 1)
+        assert flag == 0, flag
+        if table is None:
+            Bi, Be = ct.POINTER(_Table)(), ct.POINTER(_Table)()
+            assert L.ARKStepGetCurrentButcherTables(mem, ct.byref(Bi), ct.byref(Be)) == 0
+            assert not Be and Bi
+            table = _read_table(Bi.contents)
+        row = []
+        for name in ("ARKodeGetNumSteps", "ARKodeGetNumStepAttempts"):
+            getattr(L, name)(mem, ct.byref(c))
+            row.append(c.value)
+        L.ARKodeGetNumRhsEvals(mem, 1, ct.byref(c))
+        row.append(c.value)
+        for name in ("ARKodeGetNumErrTestFails", "ARKodeGetNumStepSolveFails",
+                     "ARKodeGetNumNonlinSolvIters", "ARKodeGetNumNonlinSolvConvFails",
+                     "ARKodeGetNumLinIters", "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals",
+                     "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
+            getattr(L, name)(mem, ct.byref(c))
+            row.append(c.value)
+        rrow = []
+        for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
+                     "ARKodeGetActualInitStep"):
+            getattr(L, name)(mem, ct.byref(r))
+            rrow.append(r.value)
+        cnt.append(row)
+        real.append(rrow)
+        sols.append(prob.arr(y).copy())
+    pm = VP(mem)
+    L.ARKodeFree(ct.byref(pm))
+    L.SUNNonlinSolFree(NLS)
+    L.SUNLinSolFree(LS)
+    L.N_VDestroy(y)
+    L.SUNContext_Free(ct.byref(ctx))
+    return np.array(cnt, np.int64), np.array(real), np.array(sols), table
+
+
+def run_port(y0_handle, LS_handle, callbacks, get, touts, table, rtol, atol, mxstep=100000):
+    """The restated ARKStep DIRK on the objects it is given: y0_handle (an
+    N_Vector holding u0, also used for the outputs), LS_handle (a
+    SUNLinearSolver built on it), callbacks = (f, jtimes, psolve, user_data)
+    addresses (jtimes None: difference quotients), get(handle) -> numpy copy,
+    table = the Butcher table dict of run_reference_with."""
+    P = port_lib()
+    f, jt, pv, data = callbacks
+    A = np.ascontiguousarray(table["A"], np.float64)
+    b, c, d = (np.ascontiguousarray(table[k], np.float64) for k in ("b", "c", "d"))
+    q, p = (int(v) for v in table["orders"])
+    DP = ct.POINTER(D)
+    mem = P.arkdirk_port_create(f, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, pv, data,
+                                len(b), q, p, A.ctypes.data_as(DP), b.ctypes.data_as(DP),
+                                c.ctypes.data_as(DP), d.ctypes.data_as(DP))
+    assert mem
+    cnt, real, sols = [], [], []
+    t = D()
+    cbuf = (ct.c_long * len(COUNTER_NAMES))()
+    rbuf = (D * len(REAL_NAMES))()
+    try:
+        for tout in touts:
+            flag = P.arkdirk_port_solve(mem, tout, y0_handle, ct.byref(t))
+            assert flag == 0, flag
+            P.arkdirk_port_stats(mem, cbuf, rbuf)
+            cnt.append(list(cbuf))
+            real.append(list(rbuf))
+            sols.append(get(y0_handle))
+    finally:
+        P.arkdirk_port_free(mem)
+    return np.array(cnt, np.int64), np.array(real), np.array(sols)
+
+
+def run_port_serial_with(make_serial, u0, touts, table, rtol, atol):
+    """run_port on the reference's own serial vector and SPGMR (the pin)."""
+    L = ref_lib()
+    ctx = VP()
+    assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
+    prob = make_serial(L)
+    y = L.N_VNew_Serial(len(u0), ctx)
+    prob.arr(y)[:] = u0
+    LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    f, jt, _, pv = prob.addresses()
+    try:
+        return run_port(y, LS, (f, jt, pv, None), lambda h: prob.arr(h).copy(), touts, table,
+                        rtol, atol)
+    finally:
+        L.SUNLinSolFree(LS)
+        L.N_VDestroy(y)
+        L.SUNContext_Free(ct.byref(ctx))

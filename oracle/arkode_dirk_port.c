@@ -1,0 +1,924 @@
+/* arkode_dirk_port.c -- TEST ORACLE (checker only, never part of the product).
+ *
+ * ARKODE's ARKStep with an implicit right-hand side only (a DIRK method),
+ * the Newton nonlinear solver and a matrix-free iterative SUNLinearSolver
+ * (user or difference-quotient Jacobian-times-vector, a preconditioner solve
+ * without a preconditioner setup) -- the ARK-DIRK configuration of the 3-D
+ * advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
+ * arkode_driver.cpp:51-160) -- restated over the generic object model: every
+ * vector operation is dispatched through the vector's ops table (fused
+ * operations when the vector provides them, the reference's fallback
+ * compositions otherwise) and the linear solver is driven only through its
+ * ops table.  The same code runs the reference's own NVECTOR_SERIAL +
+ * SUNLINSOL_SPGMR (pinned bit for bit against the reference's ARKodeEvolve by
+ * tests/test_arkode_dirk_port.py) and NVECTOR_GB300 + SUNLinSol_SPGMR_GB300 on
+ * a GPU machine where the reference library is not available.
+ *
+ * The Butcher table is an input (A, b, c, d, orders), read from the
+ * reference's own table object where the reference runs, so no coefficient is
+ * restated here.
+ *
+ * Follows, in the same floating-point order (compiled with -ffp-contract=off):
+ *   ARKodeEvolve, ARK_NORMAL (no tstop, roots, constraints, relaxation)
+ *                                  src/arkode/arkode.c:657-1173
+ *   ARKodeGetDky (k = 0)           arkode.c:1175-1240
+ *   arkInitialSetup                arkode.c:1978-2250
+ *   arkStopTests (tout reached)    arkode.c:2272-2470
+ *   arkHin / arkUpperBoundH0 / arkYddNorm   arkode.c:2485-2678
+ *   arkCompleteStep                arkode.c:2679-2770
+ *   arkCheckConvergence / arkCheckTemporalError   arkode.c:3207-3270, 3335-3395
+ *   arkEwtSetSS                    arkode.c:2935-2950
+ *   arkAdapt                       src/arkode/arkode_adapt.c:105-205
+ *   default controller (I)         src/sunadaptcontroller/soderlind/
+ *                                  sunadaptcontroller_soderlind.c:395-420, 566-610, 665-680
+ *   ARKodeSetDefaults / ARKStep defaults   src/arkode/arkode_io.c:48-120,
+ *                                  arkode_arkstep_io.c:735-795
+ *   arkStep_Init (implicit, FIRST_INIT)    src/arkode/arkode_arkstep.c:945-1200
+ *   arkStep_FullRHS (implicit only)        arkode_arkstep.c:1297-1660
+ *   arkStep_TakeStep_Z             arkode_arkstep.c:1666-2240
+ *   arkStep_Predict (trivial)      arkode_arkstep.c:2807-3037
+ *   arkStep_StageSetup             arkode_arkstep.c:3038-3160
+ *   arkStep_ComputeSolutions       arkode_arkstep.c:3162-3337
+ *   arkStep_Nls / NlsResidual_MassIdent / NlsLSolve / NlsConvTest
+ *                                  src/arkode/arkode_arkstep_nls.c:364-604, 1152-1200
+ *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-310
+ *   ARKodeSetLinearSolver defaults, arkLsInitialize, arkLsATimes,
+ *   arkLsDQJtimes, arkLsPSolve, arkLsSolve
+ *                                  src/arkode/arkode_ls.c:50-300, 2319-2456, 2842-2880,
+ *                                  2981-3160, 3308-3520
+ *   Hermite interpolation module (degree <= 3)   src/arkode/arkode_interp.c:97-170, 307-560
+ *   N_VLinearCombination dispatch  src/sundials/sundials_nvector.c:549-580
+ */
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/sundials_gb300_abi.h"
+
+#define UROUND DBL_EPSILON
+#define MAXS 16
+
+/* ARKODE defaults (arkode_impl.h:69-144, arkode_adapt_impl.h:43-66,
+ * arkode_arkstep_impl.h:39-52, arkode_ls_impl.h:42-43) */
+#define MAXNEF 7
+#define MAXNCF 10
+#define MAX_DQITERS 3
+#define TINY 1.0e-10
+#define FUZZ_FACTOR 100.0
+#define H0_LBFACTOR 100.0
+#define H0_UBFACTOR 0.1
+#define H0_BIAS 0.5
+#define H0_ITERS 4
+#define ONEPSM 1.000001
+#define ONEMSM 0.999999
+#define SAFETY 0.9
+#define GROWTH 20.0
+#define HFIXED_LB 1.0
+#define HFIXED_UB 1.0
+#define ETAMX1 10000.0
+#define ETAMXF 0.3
+#define ETAMIN 0.1
+#define ETACF 0.25
+#define SMALL_NEF 2
+#define MAXCOR 3
+#define CRDOWN 0.3
+#define RDIV 2.3
+#define NLSCOEF 0.1
+#define ARKLS_EPLIN 0.05
+#define INTERP_MAX_DEGREE 5
+
+enum { PREDICT_AGAIN = 3, CONV_FAIL = 4, TRY_AGAIN = 5, FIRST_CALL = 6, PREV_CONV_FAIL = 7,
+       PREV_ERR_FAIL = 8, RHSFUNC_RECVR = 9 };
+enum { NLS_CONTINUE = 901, NLS_CONV_RECVR = 902 };
+enum { FULLRHS_START = 0, FULLRHS_END = 1, FULLRHS_OTHER = 2 };
+enum { ARK_SUCCESS = 0, ARK_TOO_MUCH_WORK = -1, ARK_TOO_MUCH_ACC = -2, ARK_ERR_FAILURE = -3,
+       ARK_CONV_FAILURE = -4, ARK_LSOLVE_FAIL = -7, ARK_RHSFUNC_FAIL = -8,
+       ARK_REPTD_RHSFUNC_ERR = -10, ARK_UNREC_RHSFUNC_ERR = -11, ARK_TOO_CLOSE = -27,
+       ARK_BAD_T = -25, ARK_ILL_INPUT = -22 };
+
+/* The user callbacks, with ARKODE's signatures (arkode.h, arkode_ls.h). */
+typedef int (*ArkRhsFn)(double t, N_Vector y, N_Vector ydot, void* user_data);
+typedef int (*ArkJTimesFn)(N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vector fy,
+                           void* user_data, N_Vector tmp);
+typedef int (*ArkPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
+                           double gamma, double delta, int lr, void* user_data);
+
+typedef struct
+{
+  /* problem, options, method */
+  ArkRhsFn fi;
+  ArkJTimesFn jtimes;
+  ArkPSolveFn psolve;
+  void* user_data;
+  double rtol, atol;
+  long mxstep;
+  SUNLinearSolver LS;
+  int s, q, p, stiffly_accurate;
+  double A[MAXS][MAXS], b[MAXS], c[MAXS], d[MAXS];
+  /* vectors (ycur is the caller's output vector, as in ARKodeEvolve) */
+  N_Vector yn, fn, ycur, ewt, tempv1, tempv2, tempv3, sdata, zpred, zcor, delta;
+  N_Vector Fi[MAXS], ls_x, ls_ytemp, yold, fold;
+  /* integrator state */
+  double tn, tcur, h, hold, hprime, next_h, eta, h0u, tretlast, tolsf;
+  double etamax;
+  int initsetup, firststage, fn_is_current;
+  long nst, nst_attempts, netf, ncfn, nfi;
+  /* interpolation (Hermite) */
+  int interp_degree;
+  double hint_told, hint_tnew, hint_h;
+  /* stage / nonlinear solver */
+  int istage;
+  double gamma, gammap, gamrat, crate, delp, eRNrm;
+  int curiter;
+  long niters, nconvfails, nls_iters, nls_fails;
+  /* linear solver interface */
+  double ls_tcur, nrmfac, eplifac;
+  N_Vector ls_ycur, ls_fcur;
+  long nli, nps, njtimes, nfeDQ, ncfl;
+  /* I controller history (SUNAdaptController_UpdateH_Soderlind) */
+  double c_ep, c_hp;
+} ArkPort;
+
+/* ------------------------------------------------------ generic vector layer */
+static void v_linearsum(double a, N_Vector x, double b, N_Vector y, N_Vector z)
+{
+  z->ops->nvlinearsum(a, x, b, y, z);
+}
+static void v_const(double c, N_Vector z) { z->ops->nvconst(c, z); }
+static void v_scale(double c, N_Vector x, N_Vector z) { z->ops->nvscale(c, x, z); }
+static double v_wrms(N_Vector x, N_Vector w) { return x->ops->nvwrmsnorm(x, w); }
+
+static void v_lincomb(int nvec, double* c, N_Vector* X, N_Vector z)
+{
+  if (z->ops->nvlinearcombination) z->ops->nvlinearcombination(nvec, c, X, z);
+  else
+  {
+    z->ops->nvscale(c[0], X[0], z);
+    for (int i = 1; i < nvec; i++) z->ops->nvlinearsum(c[i], X[i], 1.0, z, z);
+  }
+}
+
+static double dmax(double a, double b) { return a > b ? a : b; }
+static double dmin(double a, double b) { return a < b ? a : b; }
+
+/* arkEwtSetSS (atol > 0, so no N_VMin test) */
+static void set_ewt(ArkPort* m, N_Vector ycur, N_Vector w)
+{
+  N_Vector t = m->tempv1;
+  t->ops->nvabs(ycur, t);
+  v_scale(m->rtol, t, t);
+  t->ops->nvaddconst(t, m->atol, t);
+  t->ops->nvinv(t, w);
+}
+
+/* arkStep_FullRHS, implicit right-hand side only, identity mass matrix */
+static int full_rhs(ArkPort* m, double t, N_Vector y, N_Vector f, int mode)
+{
+  int r;
+  switch (mode)
+  {
+  case FULLRHS_START:
+    if (!m->fn_is_current)
+    {
+      r = m->fi(t, y, m->Fi[0], m->user_data);
+      m->nfi++;
+      if (r != 0) return ARK_RHSFUNC_FAIL;
+    }
+    v_scale(1.0, m->Fi[0], f);
+    break;
+  case FULLRHS_END:
+    if (!m->fn_is_current)
+    {
+      if (!m->stiffly_accurate)
+      {
+        r = m->fi(t, y, m->Fi[0], m->user_data);
+        m->nfi++;
+        if (r != 0) return ARK_RHSFUNC_FAIL;
+      }
+      else v_scale(1.0, m->Fi[m->s - 1], m->Fi[0]);
+    }
+    v_scale(1.0, m->Fi[0], f);
+    break;
+  default:
+    r = m->fi(t, y, m->sdata, m->user_data);
+    m->nfi++;
+    if (r != 0) return ARK_RHSFUNC_FAIL;
+    v_scale(1.0, m->sdata, f);
+    break;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------ ARKLS callbacks */
+/* arkLsDQJtimes: Jv = (fi(t, y + sig v) - fy) / sig, sig = 1 / |v|_wrms */
+static int dq_jtimes(ArkPort* m, N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vector fy,
+                     N_Vector work)
+{
+  double sig = 1.0 / v_wrms(v, m->ewt);
+  int retval = 0;
+  for (int iter = 0; iter < MAX_DQITERS; iter++)
+  {
+    v_linearsum(sig, v, 1.0, y, work);
+    retval = m->fi(t, work, Jv, m->user_data);
+    m->nfeDQ++;
+    if (retval == 0) break;
+    if (retval < 0) return -1;
+    sig *= 0.25;
+  }
+  if (retval > 0) return 1;
+  const double siginv = 1.0 / sig;
+  v_linearsum(siginv, Jv, -siginv, fy, Jv);
+  return 0;
+}
+
+static int ls_atimes(void* mem, N_Vector v, N_Vector z)
+{ /* arkLsATimes (identity mass matrix) */
+  ArkPort* m = (ArkPort*)mem;
+  int r      = m->jtimes
+                 ? m->jtimes(v, z, m->ls_tcur, m->ls_ycur, m->ls_fcur, m->user_data, m->ls_ytemp)
+                 : dq_jtimes(m, v, z, m->ls_tcur, m->ls_ycur, m->ls_fcur, m->ls_ytemp);
+  m->njtimes++;
+  if (r != 0) return r;
+  v_linearsum(1.0, v, -m->gamma, z, z);
+  return 0;
+}
+
+static int ls_psolve(void* mem, N_Vector r, N_Vector z, double tol, int lr)
+{ /* arkLsPSolve */
+  ArkPort* m = (ArkPort*)mem;
+  int ret = m->psolve(m->ls_tcur, m->ls_ycur, m->ls_fcur, r, z, m->gamma, tol, lr, m->user_data);
+  m->nps++;
+  return ret;
+}
+
+/* arkLsSolve, iterative and matrix-free (rwt = ewt) */
+static int ls_solve(ArkPort* m, N_Vector b, double tnow, N_Vector ynow, N_Vector fnow,
+                    double eRNrm, int mnewt)
+{
+  m->ls_tcur        = tnow;
+  m->ls_ycur        = ynow;
+  m->ls_fcur        = fnow;
+  const double deltar = m->eplifac * eRNrm;
+  const double bnorm  = v_wrms(b, m->ewt);
+  if (bnorm <= deltar)
+  {
+    if (mnewt > 0) v_const(0.0, b);
+    return 0;
+  }
+  double delta = deltar * m->nrmfac;
+  if (m->LS->ops->setscalingvectors) m->LS->ops->setscalingvectors(m->LS, m->ewt, m->ewt);
+  else
+  {
+    v_const(1.0, m->ls_x);
+    const double rwt_mean = v_wrms(m->ewt, m->ls_x);
+    delta /= rwt_mean;
+  }
+  v_const(0.0, m->ls_x);
+  if (m->LS->ops->setzeroguess) m->LS->ops->setzeroguess(m->LS, SUNTRUE);
+  int retval = m->LS->ops->solve(m->LS, NULL, m->ls_x, b, delta);
+  v_scale(1.0, m->ls_x, b);
+  int nli_inc = m->LS->ops->numiters ? m->LS->ops->numiters(m->LS) : 0;
+  m->nli += nli_inc;
+  if (retval != 0) m->ncfl++;
+  switch (retval)
+  {
+  case 0: return 0;
+  case SUNLS_RES_REDUCED: return mnewt == 0 ? 0 : 1;
+  case SUNLS_CONV_FAIL:
+  case SUNLS_ATIMES_FAIL_REC:
+  case SUNLS_PSOLVE_FAIL_REC:
+  case SUNLS_PACKAGE_FAIL_REC:
+  case SUNLS_QRFACT_FAIL:
+  case SUNLS_LUFACT_FAIL: return 1;
+  default: return retval < 0 ? -1 : 0;
+  }
+}
+
+/* ------------------------------------------------------ Newton + ARKStep NLS */
+static int nls_residual(ArkPort* m, N_Vector zcor, N_Vector r)
+{ /* arkStep_NlsResidual_MassIdent */
+  double c[3];
+  N_Vector X[3];
+  v_linearsum(1.0, m->zpred, 1.0, zcor, m->ycur);
+  int ret = m->fi(m->tcur, m->ycur, m->Fi[m->istage], m->user_data);
+  m->nfi++;
+  if (ret < 0) return ARK_RHSFUNC_FAIL;
+  if (ret > 0) return RHSFUNC_RECVR;
+  c[0] = 1.0;
+  X[0] = zcor;
+  c[1] = -1.0;
+  X[1] = m->sdata;
+  c[2] = -m->gamma;
+  X[2] = m->Fi[m->istage];
+  v_lincomb(3, c, X, r);
+  return 0;
+}
+
+static int nls_lsolve(ArkPort* m, N_Vector b)
+{ /* arkStep_NlsLSolve */
+  int retval = ls_solve(m, b, m->tcur, m->ycur, m->Fi[m->istage], m->eRNrm, m->curiter);
+  if (retval < 0) return ARK_LSOLVE_FAIL;
+  if (retval > 0) return CONV_FAIL;
+  return 0;
+}
+
+static int nls_convtest(ArkPort* m, N_Vector del, double tol, int mcur)
+{ /* arkStep_NlsConvTest */
+  const double delnrm = v_wrms(del, m->ewt);
+  if (mcur > 0) m->crate = dmax(CRDOWN * m->crate, delnrm / m->delp);
+  const double dcon = dmin(m->crate, 1.0) * delnrm / tol;
+  if (dcon <= 1.0) return 0;
+  if ((mcur >= 1) && (delnrm > RDIV * m->delp)) return NLS_CONV_RECVR;
+  m->delp = delnrm;
+  return NLS_CONTINUE;
+}
+
+/* SUNNonlinSolSolve_Newton without a linear solver setup function (the
+ * matrix-free solver with no preconditioner setup disables it), so a
+ * recoverable failure is never retried with a fresh setup. */
+static int newton_solve(ArkPort* m, N_Vector zcor, double tol)
+{
+  N_Vector delta = m->delta;
+  int retval;
+  m->niters     = 0;
+  m->nconvfails = 0;
+  m->curiter    = 0;
+  retval        = nls_residual(m, zcor, delta);
+  if (retval == 0)
+  {
+    for (;;)
+    {
+      m->niters++;
+      v_scale(-1.0, delta, delta);
+      retval = nls_lsolve(m, delta);
+      if (retval != 0) break;
+      v_linearsum(1.0, zcor, 1.0, delta, zcor);
+      retval = nls_convtest(m, delta, tol, m->curiter);
+      m->curiter++;
+      if (retval == 0) return 0;
+      if (retval != NLS_CONTINUE) break;
+      if (m->curiter >= MAXCOR)
+      {
+        retval = NLS_CONV_RECVR;
+        break;
+      }
+      retval = nls_residual(m, zcor, delta);
+      if (retval != 0) break;
+    }
+  }
+  m->nconvfails++;
+  return retval;
+}
+
+static int nls(ArkPort* m)
+{ /* arkStep_Nls with no lsetup */
+  m->crate = 1.0;
+  v_const(0.0, m->zcor);
+  m->eRNrm   = 0.1 * NLSCOEF;
+  int retval = newton_solve(m, m->zcor, NLSCOEF);
+  m->nls_iters += m->niters;
+  m->nls_fails += m->nconvfails;
+  if (retval == 0)
+  {
+    v_linearsum(1.0, m->zcor, 1.0, m->zpred, m->ycur);
+    return ARK_SUCCESS;
+  }
+  if (retval == NLS_CONV_RECVR) return CONV_FAIL;
+  return retval;
+}
+
+/* ------------------------------------------------------ step pieces */
+static int stage_setup(ArkPort* m, int implicit)
+{ /* arkStep_StageSetup, implicit right-hand side only, identity mass */
+  double cvals[MAXS + 1];
+  N_Vector X[MAXS + 1];
+  const int i = m->istage;
+  int nvec    = 0;
+  if (implicit)
+  {
+    m->gamma = m->h * m->A[i][i];
+    if (m->firststage) m->gammap = m->gamma;
+    m->gamrat = m->firststage ? 1.0 : m->gamma / m->gammap;
+    v_linearsum(1.0, m->yn, -1.0, m->zpred, m->sdata);
+    cvals[0] = 1.0;
+    X[0]     = m->sdata;
+    nvec     = 1;
+  }
+  for (int j = 0; j < i; j++)
+  {
+    cvals[nvec] = m->h * m->A[i][j];
+    X[nvec]     = m->Fi[j];
+    nvec++;
+  }
+  v_lincomb(nvec, cvals, X, m->sdata);
+  return 0;
+}
+
+static int compute_solutions(ArkPort* m, double* dsm)
+{ /* arkStep_ComputeSolutions */
+  double cvals[MAXS + 1];
+  N_Vector X[MAXS + 1];
+  N_Vector yerr = m->tempv1;
+  int nvec;
+  *dsm = 0.0;
+  if (!m->stiffly_accurate)
+  {
+    cvals[0] = 1.0;
+    X[0]     = m->yn;
+    nvec     = 1;
+    for (int j = 0; j < m->s; j++)
+    {
+      cvals[nvec] = m->h * m->b[j];
+      X[nvec]     = m->Fi[j];
+      nvec++;
+    }
+    v_lincomb(nvec, cvals, X, m->ycur);
+  }
+  nvec = 0;
+  for (int j = 0; j < m->s; j++)
+  {
+    cvals[nvec] = m->h * (m->b[j] - m->d[j]);
+    X[nvec]     = m->Fi[j];
+    nvec++;
+  }
+  v_lincomb(nvec, cvals, X, yerr);
+  *dsm = v_wrms(yerr, m->ewt);
+  return 0;
+}
+
+static int take_step(ArkPort* m, double* dsm, int* nflag)
+{ /* arkStep_TakeStep_Z */
+  int implicit_stage = fabs(m->A[0][0]) > TINY;
+  const int is_start = implicit_stage ? 0 : 1;
+  /* the Hermite module needs fn, so it is always evaluated (or copied) */
+  if (!m->fn_is_current)
+  {
+    int r = full_rhs(m, m->tn, m->yn, m->fn, m->initsetup ? FULLRHS_START : FULLRHS_END);
+    if (r) return ARK_RHSFUNC_FAIL;
+    m->fn_is_current = SUNTRUE;
+  }
+  for (int is = is_start; is < m->s; is++)
+  {
+    m->istage      = is;
+    implicit_stage = fabs(m->A[is][is]) > TINY;
+    m->tcur        = m->tn + m->c[is] * m->h;
+    if (implicit_stage) v_scale(1.0, m->yn, m->zpred); /* trivial predictor */
+    stage_setup(m, implicit_stage);
+    if (implicit_stage)
+    {
+      *nflag = nls(m);
+      if (*nflag != ARK_SUCCESS) return TRY_AGAIN;
+    }
+    else v_linearsum(1.0, m->yn, 1.0, m->sdata, m->ycur);
+    int r = m->fi(m->tcur, m->ycur, m->Fi[is], m->user_data);
+    m->nfi++;
+    if (r < 0) return ARK_RHSFUNC_FAIL;
+    if (r > 0) return ARK_UNREC_RHSFUNC_ERR;
+  }
+  *nflag = compute_solutions(m, dsm);
+  if (*nflag < 0) return *nflag;
+  if (*nflag > 0) return TRY_AGAIN;
+  return ARK_SUCCESS;
+}
+
+static int check_convergence(ArkPort* m, int* nflag, int* ncf)
+{ /* arkCheckConvergence */
+  if (*nflag == ARK_SUCCESS) return ARK_SUCCESS;
+  m->ncfn++;
+  if (*nflag < 0)
+  {
+    if (*nflag == ARK_LSOLVE_FAIL) return ARK_LSOLVE_FAIL;
+    if (*nflag == ARK_RHSFUNC_FAIL) return ARK_RHSFUNC_FAIL;
+    return *nflag;
+  }
+  (*ncf)++;
+  m->etamax = 1.0;
+  if (*ncf == MAXNCF)
+  {
+    if (*nflag == CONV_FAIL) return ARK_CONV_FAILURE;
+    if (*nflag == RHSFUNC_RECVR) return ARK_REPTD_RHSFUNC_ERR;
+  }
+  m->eta = ETACF;
+  *nflag = PREV_CONV_FAIL;
+  return PREDICT_AGAIN;
+}
+
+/* arkAdapt with the default I controller: h_acc = h (bias dsm)^(-1/(p+1)) */
+static void adapt(ArkPort* m, double hcur, double dsm)
+{
+  const int ord   = m->p + 1;
+  const double e1 = 1.0 * dsm;
+  const double k1 = -1.0 / ord;
+  double h_acc    = hcur * pow(e1, k1);
+  h_acc *= SAFETY;
+  h_acc = dmin(fabs(h_acc), fabs(m->etamax * hcur));
+  h_acc = dmax(h_acc, fabs(ETAMIN * hcur));
+  if (dsm <= 1.0)
+  {
+    if ((h_acc > fabs(hcur * HFIXED_LB * ONEMSM)) && (h_acc < fabs(hcur * HFIXED_UB * ONEPSM)))
+      h_acc = hcur;
+  }
+  h_acc  = copysign(h_acc, hcur);
+  m->eta = h_acc / hcur;
+  m->eta = dmax(m->eta, 0.0 / fabs(hcur));           /* hmin = 0 */
+  m->eta /= dmax(1.0, fabs(hcur) * 0.0 * m->eta);    /* hmax_inv = 0 */
+}
+
+static int check_temporal_error(ArkPort* m, int* nflag, int* nef, double dsm)
+{ /* arkCheckTemporalError */
+  adapt(m, m->h, dsm);
+  m->eta = dmin(m->eta, m->etamax);
+  m->eta = dmax(m->eta, 0.0 / fabs(m->h));
+  m->eta /= dmax(1.0, fabs(m->h) * 0.0 * m->eta);
+  if (dsm <= 1.0) return ARK_SUCCESS;
+  (*nef)++;
+  m->netf++;
+  *nflag = PREV_ERR_FAIL;
+  if (*nef == MAXNEF) return ARK_ERR_FAILURE;
+  m->etamax = 1.0;
+  if (*nef >= SMALL_NEF) m->eta = dmin(m->eta, ETAMXF);
+  m->eta = dmin(m->eta, m->etamax);
+  m->eta = dmax(m->eta, 0.0 / fabs(m->h));
+  m->eta /= dmax(1.0, fabs(m->h) * 0.0 * m->eta);
+  return TRY_AGAIN;
+}
+
+static int complete_step(ArkPort* m, double dsm)
+{ /* arkCompleteStep (+ arkInterpUpdate_Hermite, SUNAdaptController_UpdateH) */
+  m->tcur = m->tn + m->h;
+  if (!m->fn_is_current)
+  {
+    if (full_rhs(m, m->tn, m->yn, m->fn, FULLRHS_START)) return ARK_RHSFUNC_FAIL;
+    m->fn_is_current = SUNTRUE;
+  }
+  v_scale(1.0, m->yn, m->yold);
+  v_scale(1.0, m->fn, m->fold);
+  m->hint_told = m->hint_tnew;
+  m->hint_tnew = m->tcur;
+  m->hint_h    = m->h;
+  v_scale(1.0, m->ycur, m->yn);
+  m->fn_is_current = SUNFALSE;
+  m->c_ep          = 1.0 * dsm;
+  m->c_hp          = m->h;
+  m->nst++;
+  m->hold       = m->h;
+  m->tn         = m->tcur;
+  m->hprime     = m->h * m->eta;
+  m->etamax     = GROWTH;
+  m->initsetup  = SUNFALSE;
+  m->firststage = SUNFALSE;
+  return ARK_SUCCESS;
+}
+
+/* ARKodeGetDky(t, 0) with the Hermite interpolant of degree min(5, deg) */
+static int get_dky(ArkPort* m, double t, N_Vector dky)
+{
+  double tfuzz = FUZZ_FACTOR * UROUND * (fabs(m->tcur) + fabs(m->hold));
+  if (m->hold < 0.0) tfuzz = -tfuzz;
+  const double tp  = m->tcur - m->hold - tfuzz;
+  const double tn1 = m->tcur + tfuzz;
+  if ((t - tp) * (t - tn1) > 0.0) return ARK_BAD_T;
+  const double tau = (t - m->tcur) / m->h;
+  if (!m->fn_is_current)
+  {
+    if (full_rhs(m, m->tn, m->yn, m->fn, FULLRHS_END)) return ARK_RHSFUNC_FAIL;
+    m->fn_is_current = SUNTRUE;
+  }
+  const int qd     = m->interp_degree < INTERP_MAX_DEGREE ? m->interp_degree : INTERP_MAX_DEGREE;
+  const double tau2 = tau * tau, tau3 = tau * tau2, h = m->hint_h;
+  double a[4];
+  N_Vector X[4];
+  switch (qd)
+  {
+  case 0: v_linearsum(0.5, m->yold, 0.5, m->yn, dky); break;
+  case 1: v_linearsum(-tau, m->yold, 1.0 + tau, m->yn, dky); break;
+  case 2:
+    a[0] = tau2;
+    a[1] = 1.0 - tau2;
+    a[2] = h * (tau2 + tau);
+    X[0] = m->yold;
+    X[1] = m->yn;
+    X[2] = m->fn;
+    v_lincomb(3, a, X, dky);
+    break;
+  case 3:
+    a[0] = 3.0 * tau2 + 2.0 * tau3;
+    a[1] = 1.0 - 3.0 * tau2 - 2.0 * tau3;
+    a[2] = h * (tau2 + tau3);
+    a[3] = h * (tau + 2.0 * tau2 + tau3);
+    X[0] = m->yold;
+    X[1] = m->yn;
+    X[2] = m->fold;
+    X[3] = m->fn;
+    v_lincomb(4, a, X, dky);
+    break;
+  default: return ARK_ILL_INPUT; /* degree > 3 (methods of order > 4) not restated */
+  }
+  return ARK_SUCCESS;
+}
+
+/* arkUpperBoundH0 */
+static double upper_bound_h0(ArkPort* m, double tdist)
+{
+  N_Vector temp1 = m->tempv1, temp2 = m->tempv2;
+  temp2->ops->nvabs(m->yn, temp2);
+  set_ewt(m, m->yn, temp1);
+  temp1->ops->nvinv(temp1, temp1);
+  v_linearsum(H0_UBFACTOR, temp2, 1.0, temp1, temp1);
+  temp2->ops->nvabs(m->fn, temp2);
+  temp1->ops->nvdiv(temp2, temp1, temp1);
+  const double hub_inv = temp1->ops->nvmaxnorm(temp1);
+  double hub           = H0_UBFACTOR * tdist;
+  if (hub * hub_inv > 1.0) hub = 1.0 / hub_inv;
+  return hub;
+}
+
+/* arkYddNorm */
+static int ydd_norm(ArkPort* m, double hg, double* yddnrm)
+{
+  v_linearsum(hg, m->fn, 1.0, m->yn, m->ycur);
+  if (full_rhs(m, m->tcur + hg, m->ycur, m->tempv1, FULLRHS_OTHER)) return ARK_RHSFUNC_FAIL;
+  v_linearsum(1.0 / hg, m->tempv1, -1.0 / hg, m->fn, m->tempv1);
+  v_scale(1.0, m->yn, m->ycur);
+  *yddnrm = v_wrms(m->tempv1, m->ewt);
+  return ARK_SUCCESS;
+}
+
+static double sun_rsqrt(double x) { return x <= 0.0 ? 0.0 : sqrt(x); } /* SUNRsqrt */
+
+/* arkHin */
+static int hin(ArkPort* m, double tout)
+{
+  const double tdiff = tout - m->tcur;
+  if (tdiff == 0.0) return ARK_TOO_CLOSE;
+  const int sign      = tdiff > 0.0 ? 1 : -1;
+  const double tdist  = fabs(tdiff);
+  const double tround = UROUND * dmax(fabs(m->tcur), fabs(tout));
+  if (tdist < 2.0 * tround) return ARK_TOO_CLOSE;
+  if (!m->fn_is_current)
+  {
+    if (full_rhs(m, m->tn, m->yn, m->fn, FULLRHS_START)) return ARK_RHSFUNC_FAIL;
+    m->fn_is_current = SUNTRUE;
+  }
+  const double hlb = H0_LBFACTOR * tround;
+  const double hub = upper_bound_h0(m, tdist);
+  double hg        = sun_rsqrt(hlb * hub);
+  if (hub < hlb)
+  {
+    m->h = sign == -1 ? -hg : hg;
+    return ARK_SUCCESS;
+  }
+  double hs = hg, hnew = hg, yddnrm = 0.0;
+  for (int count1 = 1; count1 <= H0_ITERS; count1++)
+  {
+    int hgOK = 0;
+    for (int count2 = 1; count2 <= H0_ITERS; count2++)
+    {
+      const double hgs = hg * sign;
+      int retval       = ydd_norm(m, hgs, &yddnrm);
+      if (retval < 0) return ARK_RHSFUNC_FAIL;
+      if (retval == ARK_SUCCESS)
+      {
+        hgOK = 1;
+        break;
+      }
+      hg *= 0.2;
+    }
+    if (!hgOK)
+    {
+      if (count1 <= 2) return ARK_REPTD_RHSFUNC_ERR;
+      hnew = hs;
+      break;
+    }
+    hs   = hg;
+    hnew = (yddnrm * hub * hub > 2.0) ? sun_rsqrt(2.0 / yddnrm) : sun_rsqrt(hg * hub);
+    if (count1 == H0_ITERS) break;
+    const double hrat = hnew / hg;
+    if ((hrat > 0.5) && (hrat < 2.0)) break;
+    if ((count1 > 1) && (hrat > 2.0))
+    {
+      hnew = hg;
+      break;
+    }
+    hg = hnew;
+  }
+  double h0 = H0_BIAS * hnew;
+  if (h0 < hlb) h0 = hlb;
+  if (h0 > hub) h0 = hub;
+  if (sign == -1) h0 = -h0;
+  m->h = h0;
+  return ARK_SUCCESS;
+}
+
+/* arkInitialSetup (after arkStep_Init, FIRST_INIT) */
+static int initial_setup(ArkPort* m, double tout)
+{
+  set_ewt(m, m->yn, m->ewt);
+  if (m->LS->ops->initialize && m->LS->ops->initialize(m->LS) != 0) return ARK_ILL_INPUT;
+  /* Hermite module: degree min(q - 1, 5) for q > 1 (arkStep_Init), then
+   * arkInterpInit_Hermite */
+  m->interp_degree = INTERP_MAX_DEGREE;
+  if (m->q > 1 && m->interp_degree > m->q - 1) m->interp_degree = m->q - 1;
+  else if (m->q == 1 && m->interp_degree > 1) m->interp_degree = 1;
+  m->hint_told = m->tcur;
+  m->hint_tnew = m->tcur;
+  m->hint_h    = 0.0;
+  /* initial step */
+  m->h = fabs(tout - m->tcur);
+  if (m->h == 0.0) m->h = 1.0;
+  int hflag = hin(m, tout);
+  if (hflag != ARK_SUCCESS) return hflag;
+  m->etamax = ETAMX1;
+  m->h0u    = m->h;
+  m->eta    = 1.0;
+  m->hprime = m->h;
+  return ARK_SUCCESS;
+}
+
+/* ------------------------------------------------------ public entry points */
+void* arkdirk_port_create(ArkRhsFn fi, double t0, N_Vector y0, double rtol, double atol,
+                          long mxstep, SUNLinearSolver LS, ArkJTimesFn jtimes,
+                          ArkPSolveFn psolve, void* user_data, int stages, int q, int p,
+                          const double* A, const double* b, const double* c, const double* d)
+{
+  if (stages < 1 || stages > MAXS || !psolve || !LS) return NULL;
+  ArkPort* m = (ArkPort*)calloc(1, sizeof(ArkPort));
+  if (!m) return NULL;
+  N_Vector (*clone)(N_Vector) = y0->ops->nvclone;
+  m->yn     = clone(y0);
+  m->fn     = clone(y0);
+  m->ewt    = clone(y0);
+  m->tempv1 = clone(y0);
+  m->tempv2 = clone(y0);
+  m->tempv3 = clone(y0);
+  m->sdata  = clone(y0);
+  m->zpred  = clone(y0);
+  m->zcor   = clone(y0);
+  m->delta  = clone(y0);
+  m->ls_x   = clone(y0);
+  m->ls_ytemp = clone(y0);
+  m->yold   = clone(y0);
+  m->fold   = clone(y0);
+  for (int j = 0; j < stages; j++) m->Fi[j] = clone(y0);
+  v_scale(1.0, y0, m->yn);
+  m->fi        = fi;
+  m->jtimes    = jtimes;
+  m->psolve    = psolve;
+  m->user_data = user_data;
+  m->rtol      = rtol;
+  m->atol      = atol;
+  m->mxstep    = mxstep;
+  m->LS        = LS;
+  m->s         = stages;
+  m->q         = q;
+  m->p         = p;
+  for (int i = 0; i < stages; i++)
+  {
+    for (int j = 0; j < stages; j++) m->A[i][j] = A[i * stages + j];
+    m->b[i] = b[i];
+    m->c[i] = c[i];
+    m->d[i] = d[i];
+  }
+  /* ARKodeButcherTable_IsStifflyAccurate: b equals the last row of A */
+  m->stiffly_accurate = 1;
+  for (int j = 0; j < stages; j++)
+    if (m->b[j] != m->A[stages - 1][j]) m->stiffly_accurate = 0;
+  m->tn = m->tcur = m->tretlast = t0;
+  m->initsetup  = SUNTRUE;
+  m->firststage = SUNTRUE;
+  m->eplifac    = ARKLS_EPLIN;
+  m->nrmfac     = sqrt((double)y0->ops->nvgetlength(y0));
+  m->c_ep = m->c_hp = 1.0;
+  if (LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
+  if (LS->ops->setpreconditioner) LS->ops->setpreconditioner(LS, m, NULL, ls_psolve);
+  return m;
+}
+
+/* ARKodeEvolve(tout, yout, &tret, ARK_NORMAL) */
+int arkdirk_port_solve(void* mem, double tout, N_Vector yout, double* tret)
+{
+  ArkPort* m = (ArkPort*)mem;
+  int istate = ARK_SUCCESS;
+  m->ycur    = yout;
+  if (m->initsetup)
+  {
+    m->tretlast = *tret = m->tcur;
+    int r               = initial_setup(m, tout);
+    if (r != ARK_SUCCESS) return r;
+  }
+  else if ((m->tcur - tout) * m->h >= 0.0)
+  { /* arkStopTests: tout already passed */
+    int ier = get_dky(m, tout, yout);
+    if (ier != ARK_SUCCESS) return ier;
+    m->tretlast = *tret = tout;
+    return ARK_SUCCESS;
+  }
+  long nstloc = 0;
+  for (;;)
+  {
+    m->next_h = m->h;
+    if (!m->initsetup) set_ewt(m, m->yn, m->ewt);
+    if ((m->mxstep > 0) && (nstloc >= m->mxstep))
+    {
+      istate      = ARK_TOO_MUCH_WORK;
+      m->tretlast = *tret = m->tcur;
+      v_scale(1.0, m->yn, yout);
+      break;
+    }
+    const double nrm = v_wrms(m->yn, m->ewt);
+    m->tolsf         = UROUND * nrm;
+    if (m->tolsf > 1.0)
+    {
+      istate      = ARK_TOO_MUCH_ACC;
+      m->tretlast = *tret = m->tcur;
+      v_scale(1.0, m->yn, yout);
+      m->tolsf *= 2.0;
+      break;
+    }
+    m->tolsf = 1.0;
+    if (m->hprime != m->h)
+    {
+      m->h      = m->h * m->eta;
+      m->next_h = m->h;
+    }
+    double dsm = 0.0;
+    int kflag = ARK_SUCCESS, ncf = 0, nef = 0, nflag = FIRST_CALL;
+    for (;;)
+    {
+      m->nst_attempts++;
+      kflag = take_step(m, &dsm, &nflag);
+      if (kflag < 0) break;
+      kflag = check_convergence(m, &nflag, &ncf);
+      if (kflag < 0) break;
+      if (kflag == ARK_SUCCESS)
+      {
+        kflag = check_temporal_error(m, &nflag, &nef, dsm);
+        if (kflag < 0) break;
+      }
+      if (kflag == ARK_SUCCESS) break;
+      if (fabs(m->h) <= 0.0 * ONEPSM) return ARK_ERR_FAILURE; /* hmin = 0 */
+      m->h *= m->eta;
+      m->next_h = m->hprime = m->h;
+    }
+    if (kflag == ARK_SUCCESS) kflag = complete_step(m, dsm);
+    if (kflag != ARK_SUCCESS)
+    {
+      istate      = kflag;
+      m->tretlast = *tret = m->tcur;
+      v_scale(1.0, m->yn, yout);
+      break;
+    }
+    nstloc++;
+    if ((m->tcur - tout) * m->h >= 0.0)
+    {
+      int r = get_dky(m, tout, yout);
+      if (r != ARK_SUCCESS)
+      {
+        istate = r;
+        break;
+      }
+      m->tretlast = *tret = tout;
+      m->next_h           = m->hprime;
+      istate              = ARK_SUCCESS;
+      break;
+    }
+  }
+  return istate;
+}
+
+/* counters: nst, nst_attempts, nfi, netf, ncfn, nni, nnf, nli, nps, njtimes,
+ * nfeDQ, ncfl; reals: last step, next step, current time, first step */
+void arkdirk_port_stats(void* mem, long* cnt, double* r)
+{
+  ArkPort* m = (ArkPort*)mem;
+  cnt[0]     = m->nst;
+  cnt[1]     = m->nst_attempts;
+  cnt[2]     = m->nfi;
+  cnt[3]     = m->netf;
+  cnt[4]     = m->ncfn;
+  cnt[5]     = m->nls_iters;
+  cnt[6]     = m->nls_fails;
+  cnt[7]     = m->nli;
+  cnt[8]     = m->nps;
+  cnt[9]     = m->njtimes;
+  cnt[10]    = m->nfeDQ;
+  cnt[11]    = m->ncfl;
+  r[0]       = m->hold;
+  r[1]       = m->next_h;
+  r[2]       = m->tcur;
+  r[3]       = m->h0u;
+}
+
+void arkdirk_port_free(void* mem)
+{
+  ArkPort* m = (ArkPort*)mem;
+  if (!m) return;
+  N_Vector vs[] = {m->yn,   m->fn,    m->ewt,  m->tempv1, m->tempv2,   m->tempv3, m->sdata,
+                   m->zpred, m->zcor, m->delta, m->ls_x,  m->ls_ytemp, m->yold,   m->fold};
+  for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); i++)
+    if (vs[i]) vs[i]->ops->nvdestroy(vs[i]);
+  for (int j = 0; j < m->s; j++)
+    if (m->Fi[j]) m->Fi[j]->ops->nvdestroy(m->Fi[j]);
+  free(m);
+}

@@ -176,3 +176,19 @@ def run_reference(q: Params, threads=None):
 def run_port_serial(q: Params):
     return hc.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol,
                                    q.atol)
+
+
+def run_reference_arkode(q: Params, threads=None):
+    """The benchmark's ARK-DIRK configuration (arkode_driver.cpp:51-160,
+    order 3) through the reference's ARKodeEvolve: (counters, reals,
+    solutions, Butcher table)."""
+    from . import arkode_dirk as ad
+    return ad.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
+                                 threads=threads)
+
+
+def run_port_serial_arkode(q: Params, table):
+    """The same through the ARKStep restatement on the reference's serial objects."""
+    from . import arkode_dirk as ad
+    return ad.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, table,
+                                   q.rtol, q.atol)

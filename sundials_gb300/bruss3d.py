@@ -68,6 +68,15 @@ class Bruss3D:
         return (addr("SUNBruss3D_GB300_RHS"), None, None, addr("SUNBruss3D_GB300_CVPSolve"),
                 self.p)
 
+    def arkode_callbacks(self):
+        """(ARKRhsFn for the implicit right-hand side, None (difference-quotient
+        J v), ARKLsPrecSolveFn) addresses and the user-data pointer: the
+        benchmark's ARK-DIRK configuration (arkode_driver.cpp:51-160).  The
+        preconditioner solve is the same function as CVODE's: the two
+        callback types have the same signature."""
+        f, _, _, psolve, p = self.cvode_callbacks()
+        return f, None, psolve, p
+
     def free(self) -> None:
         if self.p:
             self.lib.SUNBruss3D_GB300_Free(self.p)
