@@ -1,15 +1,16 @@
-"""TEST ORACLE (checker only): ARKStep DIRK runs (implicit right-hand side
-only, Newton, SPGMR with left preconditioning and the default maxl, the
-difference-quotient J v, a preconditioner solve without setup) -- the
-ARK-DIRK configuration of the 3-D advection-reaction benchmark
-(benchmarks/advection_reaction_3D/raja/arkode_driver.cpp:51-160, default
-order 3) -- by two drivers:
+"""TEST ORACLE (checker only): ARKStep runs with an implicit right-hand side
+(DIRK) or an explicit + implicit splitting (ARK IMEX), Newton, SPGMR with
+left preconditioning and the default maxl, the difference-quotient J v, a
+preconditioner solve without setup -- the ARK-DIRK and ARK-IMEX
+configurations of the 3-D advection-reaction benchmark
+(benchmarks/advection_reaction_3D/raja/arkode_driver.cpp:51-160, 239-370,
+default order 3) -- by two drivers:
 
 * ``run_reference_with``: the reference's own ARKodeEvolve on its
   NVECTOR_SERIAL / SUNLINSOL_SPGMR objects (``oracle/_ref``), which also
-  returns the Butcher table the run used (ARKStepGetCurrentButcherTables);
-* ``run_port``: the C restatement ``oracle/arkode_dirk_port.c`` on whatever
-  N_Vector and SUNLinearSolver it is given, with that table as an input.
+  returns the Butcher tables the run used (ARKStepGetCurrentButcherTables);
+* ``run_port``: the C restatement ``oracle/arkstep_port.c`` on whatever
+  N_Vector and SUNLinearSolver it is given, with those tables as inputs.
 
 Both return the counters after every output time (COUNTER_NAMES), the step
 sizes and times (REAL_NAMES) and the solutions there."""
@@ -23,9 +24,26 @@ from . import heat_cvode as hc
 from . import port
 
 COUNTER_NAMES = ("nst", "nst_attempts", "nfi", "netf", "ncfn", "nni", "nnf", "nli", "nps",
-                 "njtimes", "nfeDQ", "ncfl")
+                 "njtimes", "nfeDQ", "ncfl", "nfe")
 REAL_NAMES = ("hold", "hnext", "tcur", "h0u")
 TABLE_KEYS = ("A", "b", "c", "d", "orders")
+
+
+def tables_from(g, prefix=""):
+    """The tables dict of a fixture: keys <prefix>table_* (implicit) and
+    <prefix>etable_* (explicit, absent for a DIRK run)."""
+    Ti = {k: g[prefix + "table_" + k] for k in TABLE_KEYS}
+    Te = ({k: g[prefix + "etable_" + k] for k in TABLE_KEYS}
+          if prefix + "etable_A" in g else None)
+    return {"i": Ti, "e": Te}
+
+
+def tables_to_dict(tables, prefix=""):
+    """Fixture entries of a tables dict (inverse of tables_from)."""
+    out = {prefix + "table_" + k: v for k, v in tables["i"].items()}
+    if tables["e"] is not None:
+        out.update({prefix + "etable_" + k: v for k, v in tables["e"].items()})
+    return out
 
 VP, D, I, I64 = hc.VP, hc.D, hc.I, hc.I64
 
@@ -75,18 +93,18 @@ def ref_lib() -> ct.CDLL:
 
 def port_lib() -> ct.CDLL:
     L = port.lib()
-    if not getattr(L, "_arkdirk_declared", False):
+    if not getattr(L, "_arkstep_declared", False):
         DP = ct.POINTER(D)
-        L.arkdirk_port_create.restype = VP
-        L.arkdirk_port_create.argtypes = [VP, D, VP, D, D, ct.c_long, VP, VP, VP, VP, I, I, I,
-                                          DP, DP, DP, DP]
-        L.arkdirk_port_solve.restype = I
-        L.arkdirk_port_solve.argtypes = [VP, D, VP, ct.POINTER(D)]
-        L.arkdirk_port_stats.restype = None
-        L.arkdirk_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
-        L.arkdirk_port_free.restype = None
-        L.arkdirk_port_free.argtypes = [VP]
-        L._arkdirk_declared = True
+        L.arkstep_port_create.restype = VP
+        L.arkstep_port_create.argtypes = [VP, VP, D, VP, D, D, ct.c_long, VP, VP, VP, VP, I, I,
+                                          I, DP, DP, DP, DP, DP, DP, DP, DP]
+        L.arkstep_port_solve.restype = I
+        L.arkstep_port_solve.argtypes = [VP, D, VP, ct.POINTER(D)]
+        L.arkstep_port_stats.restype = None
+        L.arkstep_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
+        L.arkstep_port_free.restype = None
+        L.arkstep_port_free.argtypes = [VP]
+        L._arkstep_declared = True
     return L
 
 
@@ -98,12 +116,15 @@ def _read_table(T: _Table) -> dict:
             "d": np.array([T.d[i] for i in range(s)]), "orders": np.array([T.q, T.p])}
 
 
-def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None):
+def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None,
+                       imex=False):
     """The reference's ARKodeEvolve on the problem whose serial callbacks
     make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
-    psetup None, and .arr(N_Vector)): (counters, reals, solutions, table).
-    threads = k: NVECTOR_OPENMP on k threads instead of NVECTOR_SERIAL (its
-    reductions sum in another order)."""
+    psetup None, .imex_addresses() -> (fe, fi), and .arr(N_Vector)):
+    (counters, reals, solutions, tables) with tables = {"i": implicit table,
+    "e": explicit table or None}.  imex: ARKStepCreate(fe, fi) instead of
+    ARKStepCreate(NULL, f).  threads = k: NVECTOR_OPENMP on k threads
+    instead of NVECTOR_SERIAL (its reductions sum in another order)."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -113,7 +134,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     prob.arr(y)[:] = u0
     f, jt, ps, pv = prob.addresses()
     assert ps is None and jt is None
-    mem = L.ARKStepCreate(None, f, 0.0, y, ctx)
+    fe, fi = prob.imex_addresses() if imex else (None, f)
+    mem = L.ARKStepCreate(fe, fi, 0.0, y, ctx)
     assert mem
     assert L.ARKodeSetOrder(mem, order) == 0
     assert L.ARKodeSStolerances(mem, rtol, atol) == 0
@@ -132,8 +154,9 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         if table is None:
             Bi, Be = ct.POINTER(_Table)(), ct.POINTER(_Table)()
             assert L.ARKStepGetCurrentButcherTables(mem, ct.byref(Bi), ct.byref(Be)) == 0
-            assert not Be and Bi
-            table = _read_table(Bi.contents)
+            assert Bi and (bool(Be) == imex)
+            table = {"i": _read_table(Bi.contents),
+                     "e": _read_table(Be.contents) if imex else None}
         row = []
         for name in ("ARKodeGetNumSteps", "ARKodeGetNumStepAttempts"):
             getattr(L, name)(mem, ct.byref(c))
@@ -146,6 +169,8 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
                      "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
             getattr(L, name)(mem, ct.byref(c))
             row.append(c.value)
+        L.ARKodeGetNumRhsEvals(mem, 0, ct.byref(c))
+        row.append(c.value)
         rrow = []
         for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
                      "ARKodeGetActualInitStep"):
@@ -163,21 +188,30 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     return np.array(cnt, np.int64), np.array(real), np.array(sols), table
 
 
-def run_port(y0_handle, LS_handle, callbacks, get, touts, table, rtol, atol, mxstep=100000):
-    """The restated ARKStep DIRK on the objects it is given: y0_handle (an
+def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000):
+    """The restated ARKStep on the objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
-    SUNLinearSolver built on it), callbacks = (f, jtimes, psolve, user_data)
-    addresses (jtimes None: difference quotients), get(handle) -> numpy copy,
-    table = the Butcher table dict of run_reference_with."""
+    SUNLinearSolver built on it), callbacks = (fe, fi, jtimes, psolve,
+    user_data) addresses (fe None: implicit only; jtimes None: difference
+    quotients), get(handle) -> numpy copy, tables = the Butcher tables of
+    run_reference_with ({"i": ..., "e": ... or None})."""
     P = port_lib()
-    f, jt, pv, data = callbacks
-    A = np.ascontiguousarray(table["A"], np.float64)
-    b, c, d = (np.ascontiguousarray(table[k], np.float64) for k in ("b", "c", "d"))
-    q, p = (int(v) for v in table["orders"])
+    fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
-    mem = P.arkdirk_port_create(f, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, pv, data,
-                                len(b), q, p, A.ctypes.data_as(DP), b.ctypes.data_as(DP),
-                                c.ctypes.data_as(DP), d.ctypes.data_as(DP))
+    Ti, Te = tables["i"], tables["e"]
+    assert (fe is None) == (Te is None)
+    keep = []
+
+    def arrs(T):
+        if T is None:
+            return [None] * 4
+        a = [np.ascontiguousarray(T[k], np.float64) for k in ("A", "b", "c", "d")]
+        keep.extend(a)
+        return [x.ctypes.data_as(DP) for x in a]
+
+    q, p = (int(v) for v in Ti["orders"])
+    mem = P.arkstep_port_create(fe, fi, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, pv,
+                                data, len(Ti["b"]), q, p, *arrs(Ti), *arrs(Te))
     assert mem
     cnt, real, sols = [], [], []
     t = D()
@@ -185,18 +219,18 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, table, rtol, atol, mxs
     rbuf = (D * len(REAL_NAMES))()
     try:
         for tout in touts:
-            flag = P.arkdirk_port_solve(mem, tout, y0_handle, ct.byref(t))
+            flag = P.arkstep_port_solve(mem, tout, y0_handle, ct.byref(t))
             assert flag == 0, flag
-            P.arkdirk_port_stats(mem, cbuf, rbuf)
+            P.arkstep_port_stats(mem, cbuf, rbuf)
             cnt.append(list(cbuf))
             real.append(list(rbuf))
             sols.append(get(y0_handle))
     finally:
-        P.arkdirk_port_free(mem)
+        P.arkstep_port_free(mem)
     return np.array(cnt, np.int64), np.array(real), np.array(sols)
 
 
-def run_port_serial_with(make_serial, u0, touts, table, rtol, atol):
+def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol):
     """run_port on the reference's own serial vector and SPGMR (the pin)."""
     L = ref_lib()
     ctx = VP()
@@ -206,9 +240,10 @@ def run_port_serial_with(make_serial, u0, touts, table, rtol, atol):
     prob.arr(y)[:] = u0
     LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
     f, jt, _, pv = prob.addresses()
+    fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)
     try:
-        return run_port(y, LS, (f, jt, pv, None), lambda h: prob.arr(h).copy(), touts, table,
-                        rtol, atol)
+        return run_port(y, LS, (fe, fi, jt, pv, None), lambda h: prob.arr(h).copy(), touts,
+                        tables, rtol, atol)
     finally:
         L.SUNLinSolFree(LS)
         L.N_VDestroy(y)

@@ -1,22 +1,23 @@
-/* arkode_dirk_port.c -- TEST ORACLE (checker only, never part of the product).
+/* arkstep_port.c -- TEST ORACLE (checker only, never part of the product).
  *
- * ARKODE's ARKStep with an implicit right-hand side only (a DIRK method),
- * the Newton nonlinear solver and a matrix-free iterative SUNLinearSolver
- * (user or difference-quotient Jacobian-times-vector, a preconditioner solve
- * without a preconditioner setup) -- the ARK-DIRK configuration of the 3-D
- * advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
- * arkode_driver.cpp:51-160) -- restated over the generic object model: every
+ * ARKODE's ARKStep with an implicit right-hand side (a DIRK method) or an
+ * explicit + implicit splitting (an ARK IMEX method), the Newton nonlinear
+ * solver and a matrix-free iterative SUNLinearSolver (user or
+ * difference-quotient Jacobian-times-vector, a preconditioner solve without a
+ * preconditioner setup) -- the ARK-DIRK and ARK-IMEX configurations of the
+ * 3-D advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
+ * arkode_driver.cpp:51-160, 239-370) -- restated over the generic object model: every
  * vector operation is dispatched through the vector's ops table (fused
  * operations when the vector provides them, the reference's fallback
  * compositions otherwise) and the linear solver is driven only through its
  * ops table.  The same code runs the reference's own NVECTOR_SERIAL +
  * SUNLINSOL_SPGMR (pinned bit for bit against the reference's ARKodeEvolve by
- * tests/test_arkode_dirk_port.py) and NVECTOR_GB300 + SUNLinSol_SPGMR_GB300 on
+ * tests/test_arkstep_port.py) and NVECTOR_GB300 + SUNLinSol_SPGMR_GB300 on
  * a GPU machine where the reference library is not available.
  *
- * The Butcher table is an input (A, b, c, d, orders), read from the
- * reference's own table object where the reference runs, so no coefficient is
- * restated here.
+ * The Butcher tables are inputs (A, b, c, d, orders), read from the
+ * reference's own table objects where the reference runs, so no coefficient
+ * is restated here.
  *
  * Follows, in the same floating-point order (compiled with -ffp-contract=off):
  *   ARKodeEvolve, ARK_NORMAL (no tstop, roots, constraints, relaxation)
@@ -34,7 +35,7 @@
  *   ARKodeSetDefaults / ARKStep defaults   src/arkode/arkode_io.c:48-120,
  *                                  arkode_arkstep_io.c:735-795
  *   arkStep_Init (implicit, FIRST_INIT)    src/arkode/arkode_arkstep.c:945-1200
- *   arkStep_FullRHS (implicit only)        arkode_arkstep.c:1297-1660
+ *   arkStep_FullRHS                arkode_arkstep.c:1297-1660
  *   arkStep_TakeStep_Z             arkode_arkstep.c:1666-2240
  *   arkStep_Predict (trivial)      arkode_arkstep.c:2807-3037
  *   arkStep_StageSetup             arkode_arkstep.c:3038-3160
@@ -106,24 +107,25 @@ typedef int (*ArkPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vect
 
 typedef struct
 {
-  /* problem, options, method */
-  ArkRhsFn fi;
+  /* problem, options, method (fe NULL: no explicit partition) */
+  ArkRhsFn fe, fi;
   ArkJTimesFn jtimes;
   ArkPSolveFn psolve;
   void* user_data;
   double rtol, atol;
   long mxstep;
   SUNLinearSolver LS;
-  int s, q, p, stiffly_accurate;
-  double A[MAXS][MAXS], b[MAXS], c[MAXS], d[MAXS];
+  int s, q, p, stiffly_accurate, explicit_, sa_e, sa_i;
+  double A[MAXS][MAXS], b[MAXS], c[MAXS], d[MAXS];     /* implicit table */
+  double Ae[MAXS][MAXS], be[MAXS], ce[MAXS], de[MAXS]; /* explicit table */
   /* vectors (ycur is the caller's output vector, as in ARKodeEvolve) */
   N_Vector yn, fn, ycur, ewt, tempv1, tempv2, tempv3, sdata, zpred, zcor, delta;
-  N_Vector Fi[MAXS], ls_x, ls_ytemp, yold, fold;
+  N_Vector Fi[MAXS], Fe[MAXS], ls_x, ls_ytemp, yold, fold;
   /* integrator state */
   double tn, tcur, h, hold, hprime, next_h, eta, h0u, tretlast, tolsf;
   double etamax;
   int initsetup, firststage, fn_is_current;
-  long nst, nst_attempts, netf, ncfn, nfi;
+  long nst, nst_attempts, netf, ncfn, nfi, nfe;
   /* interpolation (Hermite) */
   int interp_degree;
   double hint_told, hint_tnew, hint_h;
@@ -172,39 +174,67 @@ static void set_ewt(ArkPort* m, N_Vector ycur, N_Vector w)
   t->ops->nvinv(t, w);
 }
 
-/* arkStep_FullRHS, implicit right-hand side only, identity mass matrix */
+/* the two partitions at (t, y) into Fe[0] / Fi[0] */
+static int eval_both(ArkPort* m, double t, N_Vector y)
+{
+  int r;
+  if (m->explicit_)
+  {
+    r = m->fe(t, y, m->Fe[0], m->user_data);
+    m->nfe++;
+    if (r != 0) return ARK_RHSFUNC_FAIL;
+  }
+  r = m->fi(t, y, m->Fi[0], m->user_data);
+  m->nfi++;
+  if (r != 0) return ARK_RHSFUNC_FAIL;
+  return 0;
+}
+
+/* f = Fi[0] (+ Fe[0]) */
+static void sum_first(ArkPort* m, N_Vector f)
+{
+  if (m->explicit_) v_linearsum(1.0, m->Fi[0], 1.0, m->Fe[0], f);
+  else v_scale(1.0, m->Fi[0], f);
+}
+
+/* arkStep_FullRHS, identity mass matrix */
 static int full_rhs(ArkPort* m, double t, N_Vector y, N_Vector f, int mode)
 {
   int r;
   switch (mode)
   {
   case FULLRHS_START:
-    if (!m->fn_is_current)
-    {
-      r = m->fi(t, y, m->Fi[0], m->user_data);
-      m->nfi++;
-      if (r != 0) return ARK_RHSFUNC_FAIL;
-    }
-    v_scale(1.0, m->Fi[0], f);
+    if (!m->fn_is_current && eval_both(m, t, y)) return ARK_RHSFUNC_FAIL;
+    sum_first(m, f);
     break;
   case FULLRHS_END:
     if (!m->fn_is_current)
     {
-      if (!m->stiffly_accurate)
+      const int recompute = (m->explicit_ && !m->sa_e) || !m->sa_i;
+      if (recompute)
       {
-        r = m->fi(t, y, m->Fi[0], m->user_data);
-        m->nfi++;
-        if (r != 0) return ARK_RHSFUNC_FAIL;
+        if (eval_both(m, t, y)) return ARK_RHSFUNC_FAIL;
       }
-      else v_scale(1.0, m->Fi[m->s - 1], m->Fi[0]);
+      else
+      {
+        if (m->explicit_) v_scale(1.0, m->Fe[m->s - 1], m->Fe[0]);
+        v_scale(1.0, m->Fi[m->s - 1], m->Fi[0]);
+      }
     }
-    v_scale(1.0, m->Fi[0], f);
+    sum_first(m, f);
     break;
   default:
+    if (m->explicit_)
+    {
+      r = m->fe(t, y, m->tempv2, m->user_data);
+      m->nfe++;
+      if (r != 0) return ARK_RHSFUNC_FAIL;
+    }
     r = m->fi(t, y, m->sdata, m->user_data);
     m->nfi++;
     if (r != 0) return ARK_RHSFUNC_FAIL;
-    v_scale(1.0, m->sdata, f);
+    if (m->explicit_) v_linearsum(1.0, m->sdata, 1.0, m->tempv2, f);
+    else v_scale(1.0, m->sdata, f);
     break;
   }
   return 0;
@@ -390,9 +420,9 @@ static int nls(ArkPort* m)
 
 /* ------------------------------------------------------ step pieces */
 static int stage_setup(ArkPort* m, int implicit)
-{ /* arkStep_StageSetup, implicit right-hand side only, identity mass */
-  double cvals[MAXS + 1];
-  N_Vector X[MAXS + 1];
+{ /* arkStep_StageSetup, identity mass */
+  double cvals[2 * MAXS + 2];
+  N_Vector X[2 * MAXS + 2];
   const int i = m->istage;
   int nvec    = 0;
   if (implicit)
@@ -405,6 +435,13 @@ static int stage_setup(ArkPort* m, int implicit)
     X[0]     = m->sdata;
     nvec     = 1;
   }
+  if (m->explicit_)
+    for (int j = 0; j < i; j++)
+    {
+      cvals[nvec] = m->h * m->Ae[i][j];
+      X[nvec]     = m->Fe[j];
+      nvec++;
+    }
   for (int j = 0; j < i; j++)
   {
     cvals[nvec] = m->h * m->A[i][j];
@@ -417,8 +454,8 @@ static int stage_setup(ArkPort* m, int implicit)
 
 static int compute_solutions(ArkPort* m, double* dsm)
 { /* arkStep_ComputeSolutions */
-  double cvals[MAXS + 1];
-  N_Vector X[MAXS + 1];
+  double cvals[2 * MAXS + 2];
+  N_Vector X[2 * MAXS + 2];
   N_Vector yerr = m->tempv1;
   int nvec;
   *dsm = 0.0;
@@ -429,6 +466,12 @@ static int compute_solutions(ArkPort* m, double* dsm)
     nvec     = 1;
     for (int j = 0; j < m->s; j++)
     {
+      if (m->explicit_)
+      {
+        cvals[nvec] = m->h * m->be[j];
+        X[nvec]     = m->Fe[j];
+        nvec++;
+      }
       cvals[nvec] = m->h * m->b[j];
       X[nvec]     = m->Fi[j];
       nvec++;
@@ -438,6 +481,12 @@ static int compute_solutions(ArkPort* m, double* dsm)
   nvec = 0;
   for (int j = 0; j < m->s; j++)
   {
+    if (m->explicit_)
+    {
+      cvals[nvec] = m->h * (m->be[j] - m->de[j]);
+      X[nvec]     = m->Fe[j];
+      nvec++;
+    }
     cvals[nvec] = m->h * (m->b[j] - m->d[j]);
     X[nvec]     = m->Fi[j];
     nvec++;
@@ -475,6 +524,13 @@ static int take_step(ArkPort* m, double* dsm, int* nflag)
     m->nfi++;
     if (r < 0) return ARK_RHSFUNC_FAIL;
     if (r > 0) return ARK_UNREC_RHSFUNC_ERR;
+    if (m->explicit_)
+    {
+      r = m->fe(m->tn + m->ce[is] * m->h, m->ycur, m->Fe[is], m->user_data);
+      m->nfe++;
+      if (r < 0) return ARK_RHSFUNC_FAIL;
+      if (r > 0) return ARK_UNREC_RHSFUNC_ERR;
+    }
   }
   *nflag = compute_solutions(m, dsm);
   if (*nflag < 0) return *nflag;
@@ -737,10 +793,14 @@ static int initial_setup(ArkPort* m, double tout)
 }
 
 /* ------------------------------------------------------ public entry points */
-void* arkdirk_port_create(ArkRhsFn fi, double t0, N_Vector y0, double rtol, double atol,
-                          long mxstep, SUNLinearSolver LS, ArkJTimesFn jtimes,
+/* fe NULL: implicit only (DIRK); else Ae/be/ce/de is the explicit table of
+ * the ARK pair (same number of stages); q, p: the implicit table's orders. */
+void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, double rtol,
+                          double atol, long mxstep, SUNLinearSolver LS, ArkJTimesFn jtimes,
                           ArkPSolveFn psolve, void* user_data, int stages, int q, int p,
-                          const double* A, const double* b, const double* c, const double* d)
+                          const double* A, const double* b, const double* c, const double* d,
+                          const double* Ae, const double* be, const double* ce,
+                          const double* de)
 {
   if (stages < 1 || stages > MAXS || !psolve || !LS) return NULL;
   ArkPort* m = (ArkPort*)calloc(1, sizeof(ArkPort));
@@ -761,7 +821,11 @@ void* arkdirk_port_create(ArkRhsFn fi, double t0, N_Vector y0, double rtol, doub
   m->yold   = clone(y0);
   m->fold   = clone(y0);
   for (int j = 0; j < stages; j++) m->Fi[j] = clone(y0);
+  if (fe)
+    for (int j = 0; j < stages; j++) m->Fe[j] = clone(y0);
   v_scale(1.0, y0, m->yn);
+  m->fe        = fe;
+  m->explicit_ = fe != NULL;
   m->fi        = fi;
   m->jtimes    = jtimes;
   m->psolve    = psolve;
@@ -779,11 +843,22 @@ void* arkdirk_port_create(ArkRhsFn fi, double t0, N_Vector y0, double rtol, doub
     m->b[i] = b[i];
     m->c[i] = c[i];
     m->d[i] = d[i];
+    if (fe)
+    {
+      for (int j = 0; j < stages; j++) m->Ae[i][j] = Ae[i * stages + j];
+      m->be[i] = be[i];
+      m->ce[i] = ce[i];
+      m->de[i] = de[i];
+    }
   }
   /* ARKodeButcherTable_IsStifflyAccurate: b equals the last row of A */
-  m->stiffly_accurate = 1;
+  m->sa_i = m->sa_e = 1;
   for (int j = 0; j < stages; j++)
-    if (m->b[j] != m->A[stages - 1][j]) m->stiffly_accurate = 0;
+  {
+    if (m->b[j] != m->A[stages - 1][j]) m->sa_i = 0;
+    if (fe && m->be[j] != m->Ae[stages - 1][j]) m->sa_e = 0;
+  }
+  m->stiffly_accurate = m->sa_i && (!fe || m->sa_e);
   m->tn = m->tcur = m->tretlast = t0;
   m->initsetup  = SUNTRUE;
   m->firststage = SUNTRUE;
@@ -796,7 +871,7 @@ void* arkdirk_port_create(ArkRhsFn fi, double t0, N_Vector y0, double rtol, doub
 }
 
 /* ARKodeEvolve(tout, yout, &tret, ARK_NORMAL) */
-int arkdirk_port_solve(void* mem, double tout, N_Vector yout, double* tret)
+int arkstep_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 {
   ArkPort* m = (ArkPort*)mem;
   int istate = ARK_SUCCESS;
@@ -888,8 +963,8 @@ int arkdirk_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 }
 
 /* counters: nst, nst_attempts, nfi, netf, ncfn, nni, nnf, nli, nps, njtimes,
- * nfeDQ, ncfl; reals: last step, next step, current time, first step */
-void arkdirk_port_stats(void* mem, long* cnt, double* r)
+ * nfeDQ, ncfl, nfe; reals: last step, next step, current time, first step */
+void arkstep_port_stats(void* mem, long* cnt, double* r)
 {
   ArkPort* m = (ArkPort*)mem;
   cnt[0]     = m->nst;
@@ -904,13 +979,14 @@ void arkdirk_port_stats(void* mem, long* cnt, double* r)
   cnt[9]     = m->njtimes;
   cnt[10]    = m->nfeDQ;
   cnt[11]    = m->ncfl;
+  cnt[12]    = m->nfe;
   r[0]       = m->hold;
   r[1]       = m->next_h;
   r[2]       = m->tcur;
   r[3]       = m->h0u;
 }
 
-void arkdirk_port_free(void* mem)
+void arkstep_port_free(void* mem)
 {
   ArkPort* m = (ArkPort*)mem;
   if (!m) return;
@@ -919,6 +995,9 @@ void arkdirk_port_free(void* mem)
   for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); i++)
     if (vs[i]) vs[i]->ops->nvdestroy(vs[i]);
   for (int j = 0; j < m->s; j++)
+  {
     if (m->Fi[j]) m->Fi[j]->ops->nvdestroy(m->Fi[j]);
+    if (m->Fe[j]) m->Fe[j]->ops->nvdestroy(m->Fe[j]);
+  }
   free(m);
 }

@@ -160,12 +160,25 @@ class SerialBruss:
             arr(z)[:] = solve_reaction(q, arr(y), arr(r), gamma)
             return 0
 
-        self.cbs = (hc.RHS_FN(f), hc.PSOLVE_FN(psolve))
+        def fe(t, y, ydot, data):
+            arr(ydot)[:] = advection(q, arr(y))
+            return 0
+
+        def fi(t, y, ydot, data):
+            arr(ydot)[:] = reaction(q, arr(y))
+            return 0
+
+        self.cbs = (hc.RHS_FN(f), hc.PSOLVE_FN(psolve), hc.RHS_FN(fe), hc.RHS_FN(fi))
         self.arr = arr
 
     def addresses(self):
-        f, ps = (hc.ct.cast(c, hc.VP).value for c in self.cbs)
+        f, ps = (hc.ct.cast(c, hc.VP).value for c in self.cbs[:2])
         return (f, None, None, ps)
+
+    def imex_addresses(self):
+        """(Advection, Reaction): the ARK-IMEX splitting (arkode_driver.cpp:
+        255-258, add_reactions false: Reaction = 0 + g)."""
+        return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs[2:])
 
 
 def run_reference(q: Params, threads=None):
@@ -178,17 +191,17 @@ def run_port_serial(q: Params):
                                    q.atol)
 
 
-def run_reference_arkode(q: Params, threads=None):
-    """The benchmark's ARK-DIRK configuration (arkode_driver.cpp:51-160,
-    order 3) through the reference's ARKodeEvolve: (counters, reals,
-    solutions, Butcher table)."""
-    from . import arkode_dirk as ad
-    return ad.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
-                                 threads=threads)
+def run_reference_arkode(q: Params, threads=None, imex=False, order=3):
+    """The benchmark's ARK-DIRK (arkode_driver.cpp:51-160) or, imex, ARK-IMEX
+    (239-370) configuration through the reference's ARKodeEvolve:
+    (counters, reals, solutions, Butcher tables)."""
+    from . import arkstep as ak
+    return ak.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
+                                 order=order, threads=threads, imex=imex)
 
 
-def run_port_serial_arkode(q: Params, table):
+def run_port_serial_arkode(q: Params, tables):
     """The same through the ARKStep restatement on the reference's serial objects."""
-    from . import arkode_dirk as ad
-    return ad.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, table,
+    from . import arkstep as ak
+    return ak.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, tables,
                                    q.rtol, q.atol)

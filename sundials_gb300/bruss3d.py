@@ -68,14 +68,19 @@ class Bruss3D:
         return (addr("SUNBruss3D_GB300_RHS"), None, None, addr("SUNBruss3D_GB300_CVPSolve"),
                 self.p)
 
-    def arkode_callbacks(self):
-        """(ARKRhsFn for the implicit right-hand side, None (difference-quotient
-        J v), ARKLsPrecSolveFn) addresses and the user-data pointer: the
-        benchmark's ARK-DIRK configuration (arkode_driver.cpp:51-160).  The
-        preconditioner solve is the same function as CVODE's: the two
-        callback types have the same signature."""
+    def arkode_callbacks(self, imex: bool = False):
+        """(fe, fi ARKRhsFn, None (difference-quotient J v), ARKLsPrecSolveFn)
+        addresses and the user-data pointer: the benchmark's ARK-DIRK
+        configuration (arkode_driver.cpp:51-160: fe None, fi = advection +
+        reaction) or, imex, its ARK-IMEX one (239-370: fe = advection, fi =
+        reaction).  The preconditioner solve is the same function as CVODE's:
+        the two callback types have the same signature."""
+        addr = lambda name: ct.cast(getattr(self.lib, name), ct.c_void_p).value
         f, _, _, psolve, p = self.cvode_callbacks()
-        return f, None, psolve, p
+        if imex:
+            return (addr("SUNBruss3D_GB300_Advection"), addr("SUNBruss3D_GB300_Reaction"), None,
+                    psolve, p)
+        return None, f, None, psolve, p
 
     def free(self) -> None:
         if self.p:

@@ -1,0 +1,52 @@
+"""GPU: the 3-D advection-reaction benchmark's ARKODE configurations --
+ARK-DIRK (its default, arkode_driver.cpp:51-160: implicit advection +
+reaction) and ARK-IMEX (239-370: explicit advection, implicit reaction), order
+3 -- with the GB300 modules plugged in: NVECTOR_GB300 for every vector,
+SUNLinSol_SPGMR_GB300 (left preconditioning, maxl 5) as the linear solver,
+and the device user functions of include/bruss3d_gb300.h as the right-hand
+sides and the preconditioner solve.  Driven by the ARKStep restatement
+oracle/arkstep_port.c (the reference's ARKodeEvolve bit for bit on serial
+objects: tests/test_arkstep_port.py) with the reference's Butcher tables
+from the fixture, and compared with the reference's own runs
+(tests/golden/bruss3d_arkode_ref.npz).  The reference's own runs on
+NVECTOR_OPENMP at 2-16 threads never moved a counter, so every counter after
+every output must equal the reference's; the last solution within 3x the
+reference's own weighted RMS deviation (in units of the tolerance)."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import arkstep as ak
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden" / "bruss3d_arkode_ref.npz"
+
+
+@pytest.mark.parametrize("name", ["dirk_", "imex_"])
+@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_arkstep_bruss3d_matches_reference(name, fused, fma):
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.spgmr import PREC_LEFT, SPGMR
+    g = np.load(GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    tables = ak.tables_from(g, name)
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    assert S.set_fused(fused) == 0
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        cbs = P.arkode_callbacks(imex=tables["e"] is not None)
+        c, r, s = ak.run_port(y.v, S.S, cbs, lambda h: y.get(), [float(t) for t in g["touts"]],
+                              tables, rtol, atol)
+    finally:
+        S.free()
+        P.free()
+    ref = g[name + "counters"]
+    assert np.array_equal(c, ref), dict(zip(ak.COUNTER_NAMES, (c[-1] - ref[-1]).tolist()))
+    yr = g[name + "y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g[name + "omp_wrms"].max()), 1e-6), w
