@@ -46,7 +46,9 @@ SUNGB300_EXPORT void SUNBruss3D_GB300_Free(SUNBruss3D_GB300 p);
 SUNGB300_EXPORT int SUNBruss3D_GB300_Advection(sunrealtype t, N_Vector y, N_Vector ydot, void* p);
 SUNGB300_EXPORT int SUNBruss3D_GB300_Reaction(sunrealtype t, N_Vector y, N_Vector ydot, void* p);
 SUNGB300_EXPORT int SUNBruss3D_GB300_RHS(sunrealtype t, N_Vector y, N_Vector ydot, void* p);
-/* x = (I - gamma dg/dy)^{-1} b per cell, at the state y. */
+/* x = (I - gamma dg/dy)^{-1} b per cell, at the state y; x may be b (the
+ * in-place linear solve of the benchmark's task-local Newton,
+ * arkode_driver.cpp:580-596). */
 SUNGB300_EXPORT int SUNBruss3D_GB300_SolveReaction(N_Vector y, N_Vector x, N_Vector b,
                                                    sunrealtype gamma, void* p);
 /* CVLsPrecSolveFn / ARKLsPrecSolveFn (same signature): z = (I - gamma

@@ -24,7 +24,7 @@ from . import heat_cvode as hc
 from . import port
 
 COUNTER_NAMES = ("nst", "nst_attempts", "nfi", "netf", "ncfn", "nni", "nnf", "nli", "nps",
-                 "njtimes", "nfeDQ", "ncfl", "nfe")
+                 "njtimes", "nfeDQ", "ncfl", "nfe", "nnlfi")
 REAL_NAMES = ("hold", "hnext", "tcur", "h0u")
 TABLE_KEYS = ("A", "b", "c", "d", "orders")
 
@@ -73,6 +73,18 @@ def ref_lib() -> ct.CDLL:
         ("ARKStepGetCurrentButcherTables", I, [VP, ct.POINTER(ct.POINTER(_Table)),
                                                ct.POINTER(ct.POINTER(_Table))]),
         ("ARKodeGetNumRhsEvals", I, [VP, I, ct.POINTER(ct.c_long)]),
+        ("ARKodeGetNonlinearSystemData", I, [VP, ct.POINTER(D), ct.POINTER(VP), ct.POINTER(VP),
+                                             ct.POINTER(VP), ct.POINTER(D), ct.POINTER(VP),
+                                             ct.POINTER(VP)]),
+        ("SUNNonlinSolNewEmpty", VP, [VP]),
+        ("SUNNonlinSolFreeEmpty", None, [VP]),
+        ("SUNNonlinSolSetSysFn", I, [VP, VP]),
+        ("SUNNonlinSolSetLSolveFn", I, [VP, VP]),
+        ("SUNNonlinSolSetConvTestFn", I, [VP, VP, VP]),
+        ("SUNNonlinSolInitialize", I, [VP]),
+        ("SUNNonlinSolSolve", I, [VP, VP, VP, VP, D, I, VP]),
+        ("N_VLinearSum", None, [D, VP, D, VP, VP]),
+        ("N_VLinearCombination", I, [I, ct.POINTER(D), ct.POINTER(VP), VP]),
     ]:
         f = getattr(L, name)
         f.restype, f.argtypes = res, args
@@ -104,8 +116,105 @@ def port_lib() -> ct.CDLL:
         L.arkstep_port_stats.argtypes = [VP, ct.POINTER(ct.c_long), ct.POINTER(D)]
         L.arkstep_port_free.restype = None
         L.arkstep_port_free.argtypes = [VP]
+        L.arkstep_port_set_task_local.restype = None
+        L.arkstep_port_set_task_local.argtypes = [VP, VP]
         L._arkstep_declared = True
     return L
+
+
+class _NLSOps(ct.Structure):
+    """struct _generic_SUNNonlinearSolver_Ops (sundials_nonlinearsolver.h)."""
+    _fields_ = [(n, VP) for n in ("gettype", "initialize", "setup", "solve", "free", "setsysfn",
+                                  "setlsetupfn", "setlsolvefn", "setctestfn", "setoptions",
+                                  "setmaxiters", "getnumiters", "getcuriter",
+                                  "getnumconvfails")]
+
+
+class _NLS(ct.Structure):
+    _fields_ = [("content", VP), ("ops", ct.POINTER(_NLSOps)), ("sunctx", VP)]
+
+
+_GETTYPE = ct.CFUNCTYPE(I, VP)
+_INIT = ct.CFUNCTYPE(I, VP)
+_SOLVE = ct.CFUNCTYPE(I, VP, VP, VP, VP, D, I, VP)
+_SETSYS = ct.CFUNCTYPE(I, VP, VP)
+_SETCTEST = ct.CFUNCTYPE(I, VP, VP, VP)
+_GETNCF = ct.CFUNCTYPE(I, VP, ct.POINTER(ct.c_long))
+_SYSFN = ct.CFUNCTYPE(I, VP, VP, VP)
+_LSOLVEFN = ct.CFUNCTYPE(I, VP, VP)
+
+
+class TaskLocalNewton:
+    """The 3-D advection-reaction benchmark's TaskLocalNewton
+    (arkode_driver.cpp:546-780) on one task, restated around the reference's
+    own SUNNonlinSol_Newton: a SUNNonlinearSolver of type ROOTFIND whose
+    initialize installs TaskLocalNlsResidual / TaskLocalLSolve on the inner
+    Newton, whose solve returns the inner status (the MPI reductions over one
+    task are the identity) and counts CONV_RECVR returns, and which forwards
+    the system and convergence-test functions to the inner Newton.
+    reaction(t, z, Fi) and block_solve(z, x, b, gamma) act on N_Vector
+    handles (the benchmark's Reaction and SolveReactionLinSys)."""
+
+    def __init__(self, L, ctx, y, reaction, block_solve):
+        self.L, self.ncnf, self.nnlfi = L, 0, 0
+        self.inner = L.SUNNonlinSol_Newton(y, ctx)
+        self.nls = L.SUNNonlinSolNewEmpty(ctx)
+        assert self.inner and self.nls
+
+        def sysfn(ycor, F, mem):
+            t, zpred, z, Fi, gamma, sdata, ud = D(), VP(), VP(), VP(), D(), VP(), VP()
+            L.ARKodeGetNonlinearSystemData(mem, ct.byref(t), ct.byref(zpred), ct.byref(z),
+                                           ct.byref(Fi), ct.byref(gamma), ct.byref(sdata),
+                                           ct.byref(ud))
+            L.N_VLinearSum(1.0, zpred, 1.0, ycor, z)
+            r = reaction(t.value, z, Fi)
+            self.nnlfi += 1
+            if r != 0:
+                return -1 if r < 0 else 1
+            c = (D * 3)(1.0, -1.0, -gamma.value)
+            X = (VP * 3)(ycor, sdata, Fi)
+            return 0 if L.N_VLinearCombination(3, c, X, F) == 0 else -1
+
+        def lsolve(delta, mem):
+            t, zpred, z, Fi, gamma, sdata, ud = D(), VP(), VP(), VP(), D(), VP(), VP()
+            L.ARKodeGetNonlinearSystemData(mem, ct.byref(t), ct.byref(zpred), ct.byref(z),
+                                           ct.byref(Fi), ct.byref(gamma), ct.byref(sdata),
+                                           ct.byref(ud))
+            return block_solve(z, delta, delta, gamma.value)
+
+        def initialize(nls):
+            L.SUNNonlinSolSetSysFn(self.inner, self._cb["sys"])
+            L.SUNNonlinSolSetLSolveFn(self.inner, self._cb["lsolve"])
+            return L.SUNNonlinSolInitialize(self.inner)
+
+        def solve(nls, y0, ycor, w, tol, call_lsetup, mem):
+            status = L.SUNNonlinSolSolve(self.inner, y0, ycor, w, tol, call_lsetup, mem)
+            if status < 0:
+                return status
+            if status == 902:  # SUN_NLS_CONV_RECVR
+                self.ncnf += 1
+            return status
+
+        def getncf(nls, out):
+            out[0] = self.ncnf
+            return 0
+
+        self._cb = {"sys": _SYSFN(sysfn), "lsolve": _LSOLVEFN(lsolve),
+                    "gettype": _GETTYPE(lambda nls: 0), "init": _INIT(initialize),
+                    "solve": _SOLVE(solve),
+                    "setsys": _SETSYS(lambda nls, fn: L.SUNNonlinSolSetSysFn(self.inner, fn)),
+                    "setctest": _SETCTEST(
+                        lambda nls, fn, data: L.SUNNonlinSolSetConvTestFn(self.inner, fn, data)),
+                    "getncf": _GETNCF(getncf)}
+        ops = ct.cast(self.nls, ct.POINTER(_NLS)).contents.ops.contents
+        for field, key in (("gettype", "gettype"), ("initialize", "init"), ("solve", "solve"),
+                           ("setsysfn", "setsys"), ("setctestfn", "setctest"),
+                           ("getnumconvfails", "getncf")):
+            setattr(ops, field, ct.cast(self._cb[key], VP).value)
+
+    def free(self):
+        self.L.SUNNonlinSolFreeEmpty(self.nls)
+        self.L.SUNNonlinSolFree(self.inner)
 
 
 def _read_table(T: _Table) -> dict:
@@ -117,13 +226,16 @@ def _read_table(T: _Table) -> dict:
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None,
-                       imex=False):
+                       imex=False, task_local=False):
     """The reference's ARKodeEvolve on the problem whose serial callbacks
     make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
     psetup None, .imex_addresses() -> (fe, fi), and .arr(N_Vector)):
     (counters, reals, solutions, tables) with tables = {"i": implicit table,
     "e": explicit table or None}.  imex: ARKStepCreate(fe, fi) instead of
-    ARKStepCreate(NULL, f).  threads = k: NVECTOR_OPENMP on k threads
+    ARKStepCreate(NULL, f).  task_local (with imex): the benchmark's
+    TaskLocalNewton (``--nls tl-newton``) instead of Newton + SPGMR, with the
+    problem's .reaction_into / .block_solve; the counters then end with its
+    nonlinear-residual evaluations.  threads = k: NVECTOR_OPENMP on k threads
     instead of NVECTOR_SERIAL (its reductions sum in another order)."""
     L = ref_lib()
     ctx = VP()
@@ -140,11 +252,18 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     assert L.ARKodeSetOrder(mem, order) == 0
     assert L.ARKodeSStolerances(mem, rtol, atol) == 0
     assert L.ARKodeSetMaxNumSteps(mem, mxstep) == 0
-    NLS = L.SUNNonlinSol_Newton(y, ctx)
-    assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
-    LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
-    assert L.ARKodeSetLinearSolver(mem, LS, None) == 0
-    assert L.ARKodeSetPreconditioner(mem, None, pv) == 0
+    TL, LS = None, None
+    if task_local:
+        assert imex
+        TL = TaskLocalNewton(L, ctx, y, prob.reaction_into, prob.block_solve)
+        NLS = TL.nls
+        assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
+    else:
+        NLS = L.SUNNonlinSol_Newton(y, ctx)
+        assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
+        LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+        assert L.ARKodeSetLinearSolver(mem, LS, None) == 0
+        assert L.ARKodeSetPreconditioner(mem, None, pv) == 0
     cnt, real, sols = [], [], []
     t, c, r = D(), ct.c_long(), D()
     table = None
@@ -167,10 +286,14 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
                      "ARKodeGetNumNonlinSolvIters", "ARKodeGetNumNonlinSolvConvFails",
                      "ARKodeGetNumLinIters", "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals",
                      "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
+            if TL and any(k in name for k in ("Lin", "Prec", "Jtimes")):
+                row.append(0)  # no linear solver attached
+                continue
             getattr(L, name)(mem, ct.byref(c))
             row.append(c.value)
         L.ARKodeGetNumRhsEvals(mem, 0, ct.byref(c))
         row.append(c.value)
+        row.append(TL.nnlfi if TL else 0)
         rrow = []
         for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
                      "ARKodeGetActualInitStep"):
@@ -181,20 +304,26 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         sols.append(prob.arr(y).copy())
     pm = VP(mem)
     L.ARKodeFree(ct.byref(pm))
-    L.SUNNonlinSolFree(NLS)
-    L.SUNLinSolFree(LS)
+    if TL:
+        TL.free()
+    else:
+        L.SUNNonlinSolFree(NLS)
+        L.SUNLinSolFree(LS)
     L.N_VDestroy(y)
     L.SUNContext_Free(ct.byref(ctx))
     return np.array(cnt, np.int64), np.array(real), np.array(sols), table
 
 
-def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000):
+def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000,
+             block_solve=None):
     """The restated ARKStep on the objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (fe, fi, jtimes, psolve,
     user_data) addresses (fe None: implicit only; jtimes None: difference
     quotients), get(handle) -> numpy copy, tables = the Butcher tables of
-    run_reference_with ({"i": ..., "e": ... or None})."""
+    run_reference_with ({"i": ..., "e": ... or None}); block_solve: the
+    address of a block solve (z, x, b, gamma, user_data) -> the task-local
+    Newton, with LS_handle and the preconditioner None."""
     P = port_lib()
     fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
@@ -213,6 +342,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     mem = P.arkstep_port_create(fe, fi, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, pv,
                                 data, len(Ti["b"]), q, p, *arrs(Ti), *arrs(Te))
     assert mem
+    if block_solve is not None:
+        P.arkstep_port_set_task_local(mem, block_solve)
     cnt, real, sols = [], [], []
     t = D()
     cbuf = (ct.c_long * len(COUNTER_NAMES))()
@@ -230,7 +361,7 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     return np.array(cnt, np.int64), np.array(real), np.array(sols)
 
 
-def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol):
+def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=False):
     """run_port on the reference's own serial vector and SPGMR (the pin)."""
     L = ref_lib()
     ctx = VP()
@@ -238,13 +369,15 @@ def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol):
     prob = make_serial(L)
     y = L.N_VNew_Serial(len(u0), ctx)
     prob.arr(y)[:] = u0
-    LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    LS = None if task_local else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
     f, jt, _, pv = prob.addresses()
     fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)
     try:
-        return run_port(y, LS, (fe, fi, jt, pv, None), lambda h: prob.arr(h).copy(), touts,
-                        tables, rtol, atol)
+        return run_port(y, LS, (fe, fi, jt, None if task_local else pv, None),
+                        lambda h: prob.arr(h).copy(), touts, tables, rtol, atol,
+                        block_solve=prob.block_solve_address() if task_local else None)
     finally:
-        L.SUNLinSolFree(LS)
+        if LS:
+            L.SUNLinSolFree(LS)
         L.N_VDestroy(y)
         L.SUNContext_Free(ct.byref(ctx))

@@ -104,6 +104,10 @@ typedef int (*ArkJTimesFn)(N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vect
                            void* user_data, N_Vector tmp);
 typedef int (*ArkPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
                            double gamma, double delta, int lr, void* user_data);
+/* the benchmark's block solve x = (I - gamma dfi/dy)^{-1} b at the state z
+ * (rhs3D.hpp SolveReactionLinSys, called with x == b) */
+typedef int (*ArkBlockSolveFn)(N_Vector z, N_Vector x, N_Vector b, double gamma,
+                               void* user_data);
 
 typedef struct
 {
@@ -111,6 +115,7 @@ typedef struct
   ArkRhsFn fe, fi;
   ArkJTimesFn jtimes;
   ArkPSolveFn psolve;
+  ArkBlockSolveFn block_lsolve; /* set: the task-local Newton, no SUNLinearSolver */
   void* user_data;
   double rtol, atol;
   long mxstep;
@@ -133,7 +138,7 @@ typedef struct
   int istage;
   double gamma, gammap, gamrat, crate, delp, eRNrm;
   int curiter;
-  long niters, nconvfails, nls_iters, nls_fails;
+  long niters, nconvfails, nls_iters, nls_fails, nnlfi, tl_ncnf;
   /* linear solver interface */
   double ls_tcur, nrmfac, eplifac;
   N_Vector ls_ycur, ls_fcur;
@@ -327,14 +332,24 @@ static int ls_solve(ArkPort* m, N_Vector b, double tnow, N_Vector ynow, N_Vector
 
 /* ------------------------------------------------------ Newton + ARKStep NLS */
 static int nls_residual(ArkPort* m, N_Vector zcor, N_Vector r)
-{ /* arkStep_NlsResidual_MassIdent */
+{ /* arkStep_NlsResidual_MassIdent; with the task-local Newton the
+   * benchmark's TaskLocalNlsResidual (arkode_driver.cpp:546-578): the same
+   * arithmetic, its evaluations counted apart, failures returned as -1 / +1 */
   double c[3];
   N_Vector X[3];
   v_linearsum(1.0, m->zpred, 1.0, zcor, m->ycur);
   int ret = m->fi(m->tcur, m->ycur, m->Fi[m->istage], m->user_data);
-  m->nfi++;
-  if (ret < 0) return ARK_RHSFUNC_FAIL;
-  if (ret > 0) return RHSFUNC_RECVR;
+  if (m->block_lsolve)
+  {
+    m->nnlfi++;
+    if (ret != 0) return ret < 0 ? -1 : 1;
+  }
+  else
+  {
+    m->nfi++;
+    if (ret < 0) return ARK_RHSFUNC_FAIL;
+    if (ret > 0) return RHSFUNC_RECVR;
+  }
   c[0] = 1.0;
   X[0] = zcor;
   c[1] = -1.0;
@@ -346,7 +361,8 @@ static int nls_residual(ArkPort* m, N_Vector zcor, N_Vector r)
 }
 
 static int nls_lsolve(ArkPort* m, N_Vector b)
-{ /* arkStep_NlsLSolve */
+{ /* arkStep_NlsLSolve; task-local: TaskLocalLSolve (arkode_driver.cpp:580-596) */
+  if (m->block_lsolve) return m->block_lsolve(m->ycur, b, b, m->gamma, m->user_data);
   int retval = ls_solve(m, b, m->tcur, m->ycur, m->Fi[m->istage], m->eRNrm, m->curiter);
   if (retval < 0) return ARK_LSOLVE_FAIL;
   if (retval > 0) return CONV_FAIL;
@@ -407,8 +423,18 @@ static int nls(ArkPort* m)
   v_const(0.0, m->zcor);
   m->eRNrm   = 0.1 * NLSCOEF;
   int retval = newton_solve(m, m->zcor, NLSCOEF);
-  m->nls_iters += m->niters;
-  m->nls_fails += m->nconvfails;
+  if (m->block_lsolve)
+  { /* TaskLocalNewton_Solve on one task (arkode_driver.cpp:615-640): the
+     * status passes through; it reports no iteration count and a running
+     * total of CONV_RECVR returns as its convergence-failure count */
+    if (retval == NLS_CONV_RECVR) m->tl_ncnf++;
+    m->nls_fails += m->tl_ncnf;
+  }
+  else
+  {
+    m->nls_iters += m->niters;
+    m->nls_fails += m->nconvfails;
+  }
   if (retval == 0)
   {
     v_linearsum(1.0, m->zcor, 1.0, m->zpred, m->ycur);
@@ -771,7 +797,8 @@ static int hin(ArkPort* m, double tout)
 static int initial_setup(ArkPort* m, double tout)
 {
   set_ewt(m, m->yn, m->ewt);
-  if (m->LS->ops->initialize && m->LS->ops->initialize(m->LS) != 0) return ARK_ILL_INPUT;
+  if (m->LS && m->LS->ops->initialize && m->LS->ops->initialize(m->LS) != 0)
+    return ARK_ILL_INPUT;
   /* Hermite module: degree min(q - 1, 5) for q > 1 (arkStep_Init), then
    * arkInterpInit_Hermite */
   m->interp_degree = INTERP_MAX_DEGREE;
@@ -802,7 +829,7 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
                           const double* Ae, const double* be, const double* ce,
                           const double* de)
 {
-  if (stages < 1 || stages > MAXS || !psolve || !LS) return NULL;
+  if (stages < 1 || stages > MAXS) return NULL;
   ArkPort* m = (ArkPort*)calloc(1, sizeof(ArkPort));
   if (!m) return NULL;
   N_Vector (*clone)(N_Vector) = y0->ops->nvclone;
@@ -865,9 +892,18 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
   m->eplifac    = ARKLS_EPLIN;
   m->nrmfac     = sqrt((double)y0->ops->nvgetlength(y0));
   m->c_ep = m->c_hp = 1.0;
-  if (LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
-  if (LS->ops->setpreconditioner) LS->ops->setpreconditioner(LS, m, NULL, ls_psolve);
+  if (LS && LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
+  if (LS && psolve && LS->ops->setpreconditioner)
+    LS->ops->setpreconditioner(LS, m, NULL, ls_psolve);
   return m;
+}
+
+/* The benchmark's TaskLocalNewton (arkode_driver.cpp:546-780) on one task:
+ * the reference's Newton with the per-cell block solve as its linear solve
+ * and no SUNLinearSolver (create with LS and psolve NULL). */
+void arkstep_port_set_task_local(void* mem, ArkBlockSolveFn block_lsolve)
+{
+  ((ArkPort*)mem)->block_lsolve = block_lsolve;
 }
 
 /* ARKodeEvolve(tout, yout, &tret, ARK_NORMAL) */
@@ -963,7 +999,7 @@ int arkstep_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 }
 
 /* counters: nst, nst_attempts, nfi, netf, ncfn, nni, nnf, nli, nps, njtimes,
- * nfeDQ, ncfl, nfe; reals: last step, next step, current time, first step */
+ * nfeDQ, ncfl, nfe, nnlfi; reals: last step, next step, current time, first step */
 void arkstep_port_stats(void* mem, long* cnt, double* r)
 {
   ArkPort* m = (ArkPort*)mem;
@@ -980,6 +1016,7 @@ void arkstep_port_stats(void* mem, long* cnt, double* r)
   cnt[10]    = m->nfeDQ;
   cnt[11]    = m->ncfl;
   cnt[12]    = m->nfe;
+  cnt[13]    = m->nnlfi;
   r[0]       = m->hold;
   r[1]       = m->next_h;
   r[2]       = m->tcur;

@@ -18,6 +18,8 @@ import numpy as np
 
 from . import heat_cvode as hc
 
+BLOCK_SOLVE_FN = hc.ct.CFUNCTYPE(hc.I, hc.VP, hc.VP, hc.VP, hc.D, hc.VP)
+
 DEFAULTS = dict(xmax=1.0, A=1.0, B=3.5, k=(1.0, 1.0, 1.0, 1.0, 1.0 / 5.0e-6, 1.0 / 5.0e-6),
                 c=0.01, rtol=1.0e-6, atol=1.0e-9, t0=0.0, tf=10.0, nout=10)
 
@@ -168,8 +170,26 @@ class SerialBruss:
             arr(ydot)[:] = reaction(q, arr(y))
             return 0
 
-        self.cbs = (hc.RHS_FN(f), hc.PSOLVE_FN(psolve), hc.RHS_FN(fe), hc.RHS_FN(fi))
+        def block_solve(z, x, b, gamma, data):
+            arr(x)[:] = solve_reaction(q, arr(z), arr(b), gamma)
+            return 0
+
+        self.cbs = (hc.RHS_FN(f), hc.PSOLVE_FN(psolve), hc.RHS_FN(fe), hc.RHS_FN(fi),
+                    BLOCK_SOLVE_FN(block_solve))
         self.arr = arr
+
+    def reaction_into(self, t, z, Fi):
+        """The benchmark's Reaction(t, z, Fi) with add_reactions false."""
+        self.arr(Fi)[:] = reaction(self.q, self.arr(z))
+        return 0
+
+    def block_solve(self, z, x, b, gamma):
+        """SolveReactionLinSys(z, x, b, gamma) (rhs3D.hpp:441-552)."""
+        self.arr(x)[:] = solve_reaction(self.q, self.arr(z), self.arr(b), gamma)
+        return 0
+
+    def block_solve_address(self):
+        return hc.ct.cast(self.cbs[4], hc.VP).value
 
     def addresses(self):
         f, ps = (hc.ct.cast(c, hc.VP).value for c in self.cbs[:2])
@@ -178,7 +198,7 @@ class SerialBruss:
     def imex_addresses(self):
         """(Advection, Reaction): the ARK-IMEX splitting (arkode_driver.cpp:
         255-258, add_reactions false: Reaction = 0 + g)."""
-        return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs[2:])
+        return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs[2:4])
 
 
 def run_reference(q: Params, threads=None):
@@ -191,17 +211,17 @@ def run_port_serial(q: Params):
                                    q.atol)
 
 
-def run_reference_arkode(q: Params, threads=None, imex=False, order=3):
+def run_reference_arkode(q: Params, threads=None, imex=False, order=3, task_local=False):
     """The benchmark's ARK-DIRK (arkode_driver.cpp:51-160) or, imex, ARK-IMEX
-    (239-370) configuration through the reference's ARKodeEvolve:
-    (counters, reals, solutions, Butcher tables)."""
+    (239-370; task_local: with --nls tl-newton) configuration through the
+    reference's ARKodeEvolve: (counters, reals, solutions, Butcher tables)."""
     from . import arkstep as ak
     return ak.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
-                                 order=order, threads=threads, imex=imex)
+                                 order=order, threads=threads, imex=imex, task_local=task_local)
 
 
-def run_port_serial_arkode(q: Params, tables):
+def run_port_serial_arkode(q: Params, tables, task_local=False):
     """The same through the ARKStep restatement on the reference's serial objects."""
     from . import arkstep as ak
     return ak.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, tables,
-                                   q.rtol, q.atol)
+                                   q.rtol, q.atol, task_local=task_local)

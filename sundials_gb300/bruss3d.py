@@ -82,6 +82,12 @@ class Bruss3D:
                     psolve, p)
         return None, f, None, psolve, p
 
+    def block_solve_address(self):
+        """SUNBruss3D_GB300_SolveReaction: the per-cell solve x = (I - gamma
+        dg/dy)^{-1} b at the state y (x may be b), the linear solve of the
+        benchmark's task-local Newton (arkode_driver.cpp:580-596)."""
+        return ct.cast(self.lib.SUNBruss3D_GB300_SolveReaction, ct.c_void_p).value
+
     def free(self) -> None:
         if self.p:
             self.lib.SUNBruss3D_GB300_Free(self.p)

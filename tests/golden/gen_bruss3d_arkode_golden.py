@@ -9,7 +9,15 @@ and SUNLINSOL_SPGMR from oracle/_ref/libsundials_ref.so, configured as the
 * ``imex_``: ARK-IMEX (239-370): explicit advection, implicit reaction;
 
 both at order 3 with Newton, SPGMR (left preconditioning, default maxl), the
-difference-quotient J v and PSolve = the per-cell reaction solve, on the
+difference-quotient J v and PSolve = the per-cell reaction solve; and
+
+* ``tl_``: ARK-IMEX with ``--nls tl-newton``: the benchmark's TaskLocalNewton
+  (546-780) on one task -- the reference's Newton with the per-cell reaction
+  solve as its linear solve and no SUNLinearSolver (the wrapper restated in
+  oracle/arkstep.py around the reference's own SUNNonlinSol_Newton: the
+  reference's build here has no MPI for the MPIPlusX vector it requires);
+
+on the
 benchmark's defaults (rtol 1e-6, atol 1e-9, t in [0, 10], 10 outputs,
 c = 0.01) on a 16^3 grid, with the user functions of
 oracle/bruss3d_cvode.py.  Stores u0, the Butcher tables each run used (read
@@ -42,14 +50,14 @@ def main():
     out = {"grid": np.array([NPTS] * 3), "touts": np.array(q.touts),
            "tol": np.array([q.rtol, q.atol]), "u0": bc.initial(q),
            "omp_threads": np.array(THREADS)}
-    for name, imex in (("dirk_", False), ("imex_", True)):
-        c, r, s, tables = bc.run_reference_arkode(q, imex=imex)
+    for name, imex, tl in (("dirk_", False, False), ("imex_", True, False), ("tl_", True, True)):
+        c, r, s, tables = bc.run_reference_arkode(q, imex=imex, task_local=tl)
         out.update({name + "counters": c, name + "reals": r, name + "y_last": s[-1],
                     **ak.tables_to_dict(tables, name)})
         print(name, dict(zip(ak.COUNTER_NAMES, c[-1].tolist())))
         oc, ow = [], []
         for th in THREADS:
-            c2, _, s2, _ = bc.run_reference_arkode(q, threads=th, imex=imex)
+            c2, _, s2, _ = bc.run_reference_arkode(q, threads=th, imex=imex, task_local=tl)
             w = 1.0 / (q.rtol * np.abs(s) + q.atol)
             oc.append(c2[-1])
             ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))

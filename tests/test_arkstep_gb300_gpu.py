@@ -4,7 +4,10 @@ reaction) and ARK-IMEX (239-370: explicit advection, implicit reaction), order
 3 -- with the GB300 modules plugged in: NVECTOR_GB300 for every vector,
 SUNLinSol_SPGMR_GB300 (left preconditioning, maxl 5) as the linear solver,
 and the device user functions of include/bruss3d_gb300.h as the right-hand
-sides and the preconditioner solve.  Driven by the ARKStep restatement
+sides and the preconditioner solve; and ARK-IMEX with the benchmark's
+task-local Newton (546-780, one task), whose linear solve is the device
+per-cell reaction solve (SUNBruss3D_GB300_SolveReaction) with no
+SUNLinearSolver at all.  Driven by the ARKStep restatement
 oracle/arkstep_port.c (the reference's ARKodeEvolve bit for bit on serial
 objects: tests/test_arkstep_port.py) with the reference's Butcher tables
 from the fixture, and compared with the reference's own runs
@@ -23,8 +26,10 @@ pytestmark = pytest.mark.gpu
 GOLDEN = Path(__file__).resolve().parent / "golden" / "bruss3d_arkode_ref.npz"
 
 
-@pytest.mark.parametrize("name", ["dirk_", "imex_"])
-@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("name,fused", [("dirk_", False), ("dirk_", True), ("imex_", False),
+                                        ("imex_", True), ("tl_", None)],
+                         ids=["dirk-unfused_gs", "dirk-fused_gs", "imex-unfused_gs",
+                              "imex-fused_gs", "imex-tl_newton"])
 @pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
 def test_arkstep_bruss3d_matches_reference(name, fused, fma):
     from sundials_gb300.bruss3d import Bruss3D
@@ -35,15 +40,19 @@ def test_arkstep_bruss3d_matches_reference(name, fused, fma):
     tables = ak.tables_from(g, name)
     y = NVector.from_numpy(g["u0"])
     y.set_fma(fma)
-    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
-    assert S.set_fused(fused) == 0
+    tl = name == "tl_"
+    S = None if tl else SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    if S:
+        assert S.set_fused(fused) == 0
     P = Bruss3D(*(int(v) for v in g["grid"]))
     try:
-        cbs = P.arkode_callbacks(imex=tables["e"] is not None)
-        c, r, s = ak.run_port(y.v, S.S, cbs, lambda h: y.get(), [float(t) for t in g["touts"]],
-                              tables, rtol, atol)
+        fe, fi, jt, psolve, data = P.arkode_callbacks(imex=tables["e"] is not None)
+        c, r, s = ak.run_port(y.v, S.S if S else None, (fe, fi, jt, None if tl else psolve, data),
+                              lambda h: y.get(), [float(t) for t in g["touts"]], tables, rtol,
+                              atol, block_solve=P.block_solve_address() if tl else None)
     finally:
-        S.free()
+        if S:
+            S.free()
         P.free()
     ref = g[name + "counters"]
     assert np.array_equal(c, ref), dict(zip(ak.COUNTER_NAMES, (c[-1] - ref[-1]).tolist()))

@@ -1,8 +1,9 @@
 """CPU: the ARKStep restatement (oracle/arkstep_port.c) against the
 reference's own ARKodeEvolve, both on the reference's NVECTOR_SERIAL and
 SUNLINSOL_SPGMR, on the 3-D advection-reaction benchmark's ARK-DIRK and
-ARK-IMEX configurations (arkode_driver.cpp:51-160, 239-370) at orders 2-4,
-with the benchmark's user functions restated in oracle/bruss3d_cvode.py:
+ARK-IMEX configurations (arkode_driver.cpp:51-160, 239-370) at orders 2-4 and
+on ARK-IMEX with its task-local Newton (546-780, one task), with the
+benchmark's user functions restated in oracle/bruss3d_cvode.py:
 every counter, step size and solution value after every output time must be
 identical, bit for bit."""
 from pathlib import Path
@@ -19,7 +20,7 @@ needs_ref = pytest.mark.skipif(not hc.REF_LIB.exists(),
                                reason="reference library not built on this machine")
 
 
-@pytest.mark.parametrize("name", ["dirk_", "imex_"])
+@pytest.mark.parametrize("name", ["dirk_", "imex_", "tl_"])
 def test_golden_layout(name):
     g = np.load(GOLDEN)
     n = 3 * int(np.prod(g["grid"]))
@@ -33,42 +34,50 @@ def test_golden_layout(name):
     # first stage explicit, lower-triangular implicit table, stiffly accurate
     assert Ti["A"][0, 0] == 0.0 and np.all(np.triu(Ti["A"], 1) == 0.0)
     assert np.array_equal(Ti["b"], Ti["A"][-1])
-    if name == "imex_":  # strictly lower-triangular explicit partner, same nodes
+    if name != "dirk_":  # strictly lower-triangular explicit partner, same nodes
         assert Te["A"].shape == (s, s) and np.all(np.triu(Te["A"]) == 0.0)
         assert np.array_equal(Te["c"], Ti["c"])
         assert g[name + "counters"][-1][ak.COUNTER_NAMES.index("nfe")] > 0
     else:
         assert Te is None
+    last = dict(zip(ak.COUNTER_NAMES, g[name + "counters"][-1]))
+    if name == "tl_":  # no SUNLinearSolver; residuals counted by the solver itself
+        assert last["nnlfi"] > 0 and last["nli"] == last["nps"] == last["nni"] == 0
+        same = dict(zip(ak.COUNTER_NAMES, g["imex_counters"][-1]))
+        assert last["nst"] == same["nst"] and last["nnlfi"] == same["nni"]
+    else:
+        assert last["nnlfi"] == 0 and last["nli"] > 0
     # the reference's own reduction-order runs never moved a counter
     assert np.all(g[name + "omp_counters"] == g[name + "counters"][-1])
 
 
 @needs_ref
-@pytest.mark.parametrize("imex", [False, True], ids=["dirk", "imex"])
+@pytest.mark.parametrize("imex,tl", [(False, False), (True, False), (True, True)],
+                         ids=["dirk", "imex", "imex_tl_newton"])
 @pytest.mark.parametrize("shape,c,order", [((6, 5, 7), 0.01, 3), ((6, 5, 7), -0.02, 4),
                                            ((5, 6, 4), 0.01, 2), ((8, 8, 8), 0.01, 3)])
-def test_port_bit_identical_to_reference(shape, c, order, imex):
+def test_port_bit_identical_to_reference(shape, c, order, imex, tl):
     q = bc.Params(*shape, c=c)
     u0 = bc.initial(q)
     c_ref, r_ref, s_ref, tables = ak.run_reference_with(lambda L: bc.SerialBruss(L, q), u0,
                                                         q.touts, q.rtol, q.atol, order=order,
-                                                        imex=imex)
+                                                        imex=imex, task_local=tl)
     c_p, r_p, s_p = ak.run_port_serial_with(lambda L: bc.SerialBruss(L, q), u0, q.touts, tables,
-                                            q.rtol, q.atol)
+                                            q.rtol, q.atol, task_local=tl)
     assert np.array_equal(c_p, c_ref), (c_p[-1] - c_ref[-1]).tolist()
     assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
     assert np.array_equal(s_p.view(np.int64), s_ref.view(np.int64))
 
 
 @needs_ref
-@pytest.mark.parametrize("name", ["dirk_", "imex_"])
+@pytest.mark.parametrize("name", ["dirk_", "imex_", "tl_"])
 def test_port_reproduces_golden(name):
     """The committed fixture (made by the reference) through the restatement,
     with the tables read from the fixture -- what the GPU test relies on."""
     g = np.load(GOLDEN)
     q = bc.Params(*(int(v) for v in g["grid"]))
     assert np.array_equal(bc.initial(q), g["u0"])
-    c, r, s = bc.run_port_serial_arkode(q, ak.tables_from(g, name))
+    c, r, s = bc.run_port_serial_arkode(q, ak.tables_from(g, name), task_local=name == "tl_")
     assert np.array_equal(c, g[name + "counters"])
     assert np.array_equal(r.view(np.int64), g[name + "reals"].view(np.int64))
     assert np.array_equal(s[-1].view(np.int64), g[name + "y_last"].view(np.int64))
