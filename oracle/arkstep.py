@@ -77,6 +77,7 @@ def ref_lib() -> ct.CDLL:
                                              ct.POINTER(VP), ct.POINTER(D), ct.POINTER(VP),
                                              ct.POINTER(VP)]),
         ("SUNNonlinSolNewEmpty", VP, [VP]),
+        ("SUNNonlinSol_FixedPoint", VP, [VP, I, VP]),
         ("SUNNonlinSolFreeEmpty", None, [VP]),
         ("SUNNonlinSolSetSysFn", I, [VP, VP]),
         ("SUNNonlinSolSetLSolveFn", I, [VP, VP]),
@@ -118,6 +119,8 @@ def port_lib() -> ct.CDLL:
         L.arkstep_port_free.argtypes = [VP]
         L.arkstep_port_set_task_local.restype = None
         L.arkstep_port_set_task_local.argtypes = [VP, VP]
+        L.arkstep_port_set_fixed_point.restype = None
+        L.arkstep_port_set_fixed_point.argtypes = [VP, I]
         L._arkstep_declared = True
     return L
 
@@ -226,7 +229,7 @@ def _read_table(T: _Table) -> dict:
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None,
-                       imex=False, task_local=False):
+                       imex=False, task_local=False, fixed_point=None):
     """The reference's ARKodeEvolve on the problem whose serial callbacks
     make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
     psetup None, .imex_addresses() -> (fe, fi), and .arr(N_Vector)):
@@ -235,7 +238,9 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     ARKStepCreate(NULL, f).  task_local (with imex): the benchmark's
     TaskLocalNewton (``--nls tl-newton``) instead of Newton + SPGMR, with the
     problem's .reaction_into / .block_solve; the counters then end with its
-    nonlinear-residual evaluations.  threads = k: NVECTOR_OPENMP on k threads
+    nonlinear-residual evaluations.  fixed_point = m: SUNNonlinSol_FixedPoint
+    with Anderson depth m and no linear solver (``--nls fixedpoint``).
+    threads = k: NVECTOR_OPENMP on k threads
     instead of NVECTOR_SERIAL (its reductions sum in another order)."""
     L = ref_lib()
     ctx = VP()
@@ -253,7 +258,11 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     assert L.ARKodeSStolerances(mem, rtol, atol) == 0
     assert L.ARKodeSetMaxNumSteps(mem, mxstep) == 0
     TL, LS = None, None
-    if task_local:
+    no_ls = task_local or fixed_point is not None
+    if fixed_point is not None:
+        NLS = L.SUNNonlinSol_FixedPoint(y, fixed_point, ctx)
+        assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
+    elif task_local:
         assert imex
         TL = TaskLocalNewton(L, ctx, y, prob.reaction_into, prob.block_solve)
         NLS = TL.nls
@@ -286,7 +295,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
                      "ARKodeGetNumNonlinSolvIters", "ARKodeGetNumNonlinSolvConvFails",
                      "ARKodeGetNumLinIters", "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals",
                      "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
-            if TL and any(k in name for k in ("Lin", "Prec", "Jtimes")):
+            if no_ls and any(k in name for k in ("Lin", "Prec", "Jtimes")):
                 row.append(0)  # no linear solver attached
                 continue
             getattr(L, name)(mem, ct.byref(c))
@@ -308,6 +317,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         TL.free()
     else:
         L.SUNNonlinSolFree(NLS)
+    if LS:
         L.SUNLinSolFree(LS)
     L.N_VDestroy(y)
     L.SUNContext_Free(ct.byref(ctx))
@@ -315,7 +325,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000,
-             block_solve=None):
+             block_solve=None, fixed_point=None):
     """The restated ARKStep on the objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (fe, fi, jtimes, psolve,
@@ -323,7 +333,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     quotients), get(handle) -> numpy copy, tables = the Butcher tables of
     run_reference_with ({"i": ..., "e": ... or None}); block_solve: the
     address of a block solve (z, x, b, gamma, user_data) -> the task-local
-    Newton, with LS_handle and the preconditioner None."""
+    Newton, with LS_handle and the preconditioner None; fixed_point = m: the
+    fixed-point solver with Anderson depth m, also without a linear solver."""
     P = port_lib()
     fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
@@ -344,6 +355,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     assert mem
     if block_solve is not None:
         P.arkstep_port_set_task_local(mem, block_solve)
+    if fixed_point is not None:
+        P.arkstep_port_set_fixed_point(mem, fixed_point)
     cnt, real, sols = [], [], []
     t = D()
     cbuf = (ct.c_long * len(COUNTER_NAMES))()
@@ -361,7 +374,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     return np.array(cnt, np.int64), np.array(real), np.array(sols)
 
 
-def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=False):
+def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=False,
+                         fixed_point=None):
     """run_port on the reference's own serial vector and SPGMR (the pin)."""
     L = ref_lib()
     ctx = VP()
@@ -369,13 +383,15 @@ def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=
     prob = make_serial(L)
     y = L.N_VNew_Serial(len(u0), ctx)
     prob.arr(y)[:] = u0
-    LS = None if task_local else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    no_ls = task_local or fixed_point is not None
+    LS = None if no_ls else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
     f, jt, _, pv = prob.addresses()
     fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)
     try:
-        return run_port(y, LS, (fe, fi, jt, None if task_local else pv, None),
+        return run_port(y, LS, (fe, fi, jt, None if no_ls else pv, None),
                         lambda h: prob.arr(h).copy(), touts, tables, rtol, atol,
-                        block_solve=prob.block_solve_address() if task_local else None)
+                        block_solve=prob.block_solve_address() if task_local else None,
+                        fixed_point=fixed_point)
     finally:
         if LS:
             L.SUNLinSolFree(LS)

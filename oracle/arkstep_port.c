@@ -4,7 +4,9 @@
  * explicit + implicit splitting (an ARK IMEX method), the Newton nonlinear
  * solver and a matrix-free iterative SUNLinearSolver (user or
  * difference-quotient Jacobian-times-vector, a preconditioner solve without a
- * preconditioner setup) -- the ARK-DIRK and ARK-IMEX configurations of the
+ * preconditioner setup), the benchmark's task-local Newton, or the
+ * fixed-point solver with Anderson acceleration (oracle/fixedpoint_port.c) --
+ * the ARK-DIRK and ARK-IMEX configurations of the
  * 3-D advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
  * arkode_driver.cpp:51-160, 239-370) -- restated over the generic object model: every
  * vector operation is dispatched through the vector's ops table (fused
@@ -56,6 +58,7 @@
 #include <string.h>
 
 #include "../include/sundials_gb300_abi.h"
+#include "fixedpoint_port.h"
 
 #define UROUND DBL_EPSILON
 #define MAXS 16
@@ -116,6 +119,7 @@ typedef struct
   ArkJTimesFn jtimes;
   ArkPSolveFn psolve;
   ArkBlockSolveFn block_lsolve; /* set: the task-local Newton, no SUNLinearSolver */
+  FPPort* fp;                   /* set: the fixed-point solver, no SUNLinearSolver */
   void* user_data;
   double rtol, atol;
   long mxstep;
@@ -417,13 +421,39 @@ static int newton_solve(ArkPort* m, N_Vector zcor, double tol)
   return retval;
 }
 
+/* arkStep_NlsFPFunction_MassIdent (arkode_arkstep_nls.c:874-900):
+ * g = gamma Fi(zpred + zcor) + sdata */
+static int fp_sys(void* mem, N_Vector zcor, N_Vector g)
+{
+  ArkPort* m = (ArkPort*)mem;
+  v_linearsum(1.0, m->zpred, 1.0, zcor, m->ycur);
+  int ret = m->fi(m->tcur, m->ycur, m->Fi[m->istage], m->user_data);
+  m->nfi++;
+  if (ret < 0) return ARK_RHSFUNC_FAIL;
+  if (ret > 0) return RHSFUNC_RECVR;
+  v_linearsum(m->gamma, m->Fi[m->istage], 1.0, m->sdata, g);
+  return 0;
+}
+
+static int fp_ctest(void* mem, N_Vector zcor, N_Vector del, double tol, int curiter)
+{
+  (void)zcor;
+  return nls_convtest((ArkPort*)mem, del, tol, curiter);
+}
+
 static int nls(ArkPort* m)
 { /* arkStep_Nls with no lsetup */
   m->crate = 1.0;
   v_const(0.0, m->zcor);
   m->eRNrm   = 0.1 * NLSCOEF;
-  int retval = newton_solve(m, m->zcor, NLSCOEF);
-  if (m->block_lsolve)
+  int retval = m->fp ? fp_port_solve(m->fp, m->zcor, NLSCOEF, fp_sys, fp_ctest, m)
+                     : newton_solve(m, m->zcor, NLSCOEF);
+  if (m->fp)
+  {
+    m->nls_iters += fp_port_niters(m->fp);
+    m->nls_fails += fp_port_nconvfails(m->fp);
+  }
+  else if (m->block_lsolve)
   { /* TaskLocalNewton_Solve on one task (arkode_driver.cpp:615-640): the
      * status passes through; it reports no iteration count and a running
      * total of CONV_RECVR returns as its convergence-failure count */
@@ -906,6 +936,14 @@ void arkstep_port_set_task_local(void* mem, ArkBlockSolveFn block_lsolve)
   ((ArkPort*)mem)->block_lsolve = block_lsolve;
 }
 
+/* ARKodeSetNonlinearSolver(SUNNonlinSol_FixedPoint(y, depth)) with no linear
+ * solver (create with LS and psolve NULL). */
+void arkstep_port_set_fixed_point(void* mem, int depth)
+{
+  ArkPort* m = (ArkPort*)mem;
+  m->fp      = fp_port_create(m->ewt, depth);
+}
+
 /* ARKodeEvolve(tout, yout, &tret, ARK_NORMAL) */
 int arkstep_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 {
@@ -1036,5 +1074,6 @@ void arkstep_port_free(void* mem)
     if (m->Fi[j]) m->Fi[j]->ops->nvdestroy(m->Fi[j]);
     if (m->Fe[j]) m->Fe[j]->ops->nvdestroy(m->Fe[j]);
   }
+  fp_port_free(m->fp);
   free(m);
 }

@@ -201,27 +201,32 @@ class SerialBruss:
         return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs[2:4])
 
 
-def run_reference(q: Params, threads=None):
+def run_reference(q: Params, threads=None, fixed_point=None):
+    """cvode_driver.cpp's CV-BDF configuration through the reference's CVode
+    (fixed_point = m: ``--nls fixedpoint --fpaccel m``)."""
     return hc.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol,
-                                 q.atol, threads=threads)
+                                 q.atol, threads=threads, fixed_point=fixed_point)
 
 
-def run_port_serial(q: Params):
+def run_port_serial(q: Params, fixed_point=None):
     return hc.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol,
-                                   q.atol)
+                                   q.atol, fixed_point=fixed_point)
 
 
-def run_reference_arkode(q: Params, threads=None, imex=False, order=3, task_local=False):
+def run_reference_arkode(q: Params, threads=None, imex=False, order=3, task_local=False,
+                         fixed_point=None):
     """The benchmark's ARK-DIRK (arkode_driver.cpp:51-160) or, imex, ARK-IMEX
     (239-370; task_local: with --nls tl-newton) configuration through the
     reference's ARKodeEvolve: (counters, reals, solutions, Butcher tables)."""
     from . import arkstep as ak
     return ak.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
-                                 order=order, threads=threads, imex=imex, task_local=task_local)
+                                 order=order, threads=threads, imex=imex, task_local=task_local,
+                                 fixed_point=fixed_point)
 
 
-def run_port_serial_arkode(q: Params, tables, task_local=False):
+def run_port_serial_arkode(q: Params, tables, task_local=False, fixed_point=None):
     """The same through the ARKStep restatement on the reference's serial objects."""
     from . import arkstep as ak
     return ak.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, tables,
-                                   q.rtol, q.atol, task_local=task_local)
+                                   q.rtol, q.atol, task_local=task_local,
+                                   fixed_point=fixed_point)

@@ -3,7 +3,8 @@
  * CVODE with BDF, the Newton nonlinear solver and either a matrix-free
  * iterative SUNLinearSolver (user or difference-quotient Jacobian-times-
  * vector, optional preconditioner) or a matrix-based direct one (SUNMatrix,
- * user Jacobian), restated
+ * user Jacobian) -- or the fixed-point nonlinear solver with Anderson
+ * acceleration and no linear solver (oracle/fixedpoint_port.c) -- restated
  * over the generic object model: every vector operation is dispatched through
  * the vector's ops table the way the reference's generic layer dispatches it
  * (fused and vector-array operations when the vector provides them, the
@@ -21,7 +22,8 @@
  *   cvHin / cvUpperBoundH0 / cvYddNorm   cvode.c:2161-2340
  *   cvStep and its callees         cvode.c:2367-3727
  *   CVodeGetDky (k = 0)            cvode.c:1671-1750
- *   cvNlsResidual / LSetup / LSolve / ConvTest   src/cvode/cvode_nls.c:256-398
+ *   cvNlsResidual / LSetup / LSolve / ConvTest / FPFunction
+ *                                  src/cvode/cvode_nls.c:256-425
  *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-330
  *   CVodeSetLinearSolver defaults, cvLsInitialize (saved J), cvLsLinSys,
  *   cvLsATimes / cvLsDQJtimes / cvLsPSetup / cvLsPSolve, cvLsSetup, cvLsSolve
@@ -35,6 +37,7 @@
 #include <string.h>
 
 #include "../include/sundials_gb300_abi.h"
+#include "fixedpoint_port.h"
 
 #define QMAX 5
 #define UROUND DBL_EPSILON
@@ -115,7 +118,8 @@ typedef struct
   sunbooleantype jbad;
   long nstlj, npe, nli, nps, ncfl, njtimes, nfeDQ, nje;
   int initialized;
-  /* Newton */
+  /* Newton, or the fixed-point solver when fp is set (no linear solver) */
+  FPPort* fp;
   int curiter;
   long niters, nconvfails;
   sunbooleantype nls_jcur;
@@ -603,9 +607,39 @@ static void set_coeffs(CvlsPort* m)
   m->gamrat = (m->nst > 0) ? m->gamma / m->gammap : 1.0;
 }
 
+/* cvNlsFPFunction (cvode_nls.c:401-425): g = rl1 (h f(tn, zn[0] + ycor) - zn[1]) */
+static int fp_sys(void* mem, N_Vector ycor, N_Vector res)
+{
+  CvlsPort* m = (CvlsPort*)mem;
+  v_linearsum(1.0, m->zn[0], 1.0, ycor, m->y);
+  int r = rhs(m, m->tn, m->y, res);
+  if (r < 0) return CV_RHSFUNC_FAIL;
+  if (r > 0) return RHSFUNC_RECVR;
+  v_linearsum(m->h, res, -1.0, m->zn[1], res);
+  v_scale(m->rl1, res, res);
+  return 0;
+}
+
+static int fp_ctest(void* mem, N_Vector ycor, N_Vector del, double tol, int curiter)
+{
+  return nls_convtest((CvlsPort*)mem, ycor, del, tol, curiter);
+}
+
 static int nls(CvlsPort* m, int nflag)
 { /* cvNls: CVLS has an lsetup only when a preconditioner setup is attached */
   int callSetup = 0;
+  if (m->fp)
+  { /* SUNNonlinSol_FixedPoint: no linear solver, so no lsetup */
+    m->crate = 1.0;
+    v_const(0.0, m->acor);
+    int flag = fp_port_solve(m->fp, m->acor, m->tq[4], fp_sys, fp_ctest, m);
+    m->nni += fp_port_niters(m->fp);
+    m->nnf += fp_port_nconvfails(m->fp);
+    if (flag != 0) return flag;
+    v_linearsum(1.0, m->zn[0], 1.0, m->acor, m->y);
+    m->cv_jcur = 0;
+    return 0;
+  }
   if (m->pset || m->A)
   {
     m->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
@@ -986,8 +1020,8 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   m->jbad      = SUNTRUE;
   m->eplifac   = CVLS_EPLIN;
   m->nrmfac    = sqrt((double)y0->ops->nvgetlength(y0));
-  if (LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
-  if (LS->ops->setpreconditioner && psolve)
+  if (LS && LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
+  if (LS && LS->ops->setpreconditioner && psolve)
     LS->ops->setpreconditioner(LS, m, pset ? ls_psetup : NULL, ls_psolve);
   return m;
 }
@@ -1000,6 +1034,15 @@ void cvls_port_set_matrix(void* mem, SUNMatrix A, CvlsJacFn jac)
   CvlsPort* m = (CvlsPort*)mem;
   m->A        = A;
   m->jac      = jac;
+}
+
+/* CVodeSetNonlinearSolver(SUNNonlinSol_FixedPoint(y, m)) with no linear
+ * solver (create the object with LS NULL): the fixed-point iteration with
+ * Anderson acceleration of depth m replaces Newton. */
+void cvls_port_set_fixed_point(void* mem, int depth)
+{
+  CvlsPort* m = (CvlsPort*)mem;
+  m->fp       = fp_port_create(m->ewt, depth);
 }
 
 /* CVodeSVtolerances(rtol, abstol): a copy of abstol is kept (all entries > 0). */
@@ -1022,7 +1065,7 @@ int cvls_port_solve(void* mem, double tout, N_Vector yout, double* tret)
     { /* cvInitialSetup: ewt, then cvLsInitialize (the saved J of a matrix) */
       set_ewt(m, m->zn[0], m->ewt);
       if (m->A && !m->savedJ) m->savedJ = m->A->ops->clone(m->A);
-      m->LS->ops->initialize(m->LS);
+      if (m->LS) m->LS->ops->initialize(m->LS);
       m->initialized = 1;
     }
     int r = rhs(m, m->tn, m->zn[0], m->zn[1]);
@@ -1119,5 +1162,6 @@ void cvls_port_free(void* mem)
   for (int j = 0; j <= QMAX; j++) m->zn[j]->ops->nvdestroy(m->zn[j]);
   if (m->Vabstol) m->Vabstol->ops->nvdestroy(m->Vabstol);
   if (m->savedJ) m->savedJ->ops->destroy(m->savedJ);
+  fp_port_free(m->fp);
   free(m);
 }

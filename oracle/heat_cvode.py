@@ -31,6 +31,9 @@ REF_LIB = Path(__file__).resolve().parent / "_ref" / "libsundials_ref.so"
 COUNTER_NAMES = ("nst", "nfe", "nni", "nnf", "ncfn", "netf", "nsetups", "nli", "npe", "nps",
                  "njtimes", "ncfl", "qu", "q", "nfels", "nje")
 REAL_NAMES = ("hu", "h", "tn", "h0u")
+# CVLS getters, which fail when no linear solver is attached
+LS_GETTERS = ("CVodeGetNumLinIters", "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves",
+              "CVodeGetNumJtimesEvals", "CVodeGetNumLinConvFails")
 
 VP, D, I, I64 = ct.c_void_p, ct.c_double, ct.c_int, ct.c_int64
 RHS_FN = ct.CFUNCTYPE(I, D, VP, VP, VP)
@@ -74,6 +77,9 @@ def ref_lib() -> ct.CDLL:
         ("CVodeSetPreconditioner", I, [VP, VP, VP]),
         ("CVode", I, [VP, D, VP, ct.POINTER(D), I]),
         ("CVodeFree", None, [ct.POINTER(VP)]),
+        ("SUNNonlinSol_FixedPoint", VP, [VP, I, VP]),
+        ("CVodeSetNonlinearSolver", I, [VP, VP]),
+        ("SUNNonlinSolFree", I, [VP]),
     ]:
         f = getattr(L, name)
         f.restype, f.argtypes = res, args
@@ -109,6 +115,8 @@ def port_lib() -> ct.CDLL:
         L.cvls_port_set_vabstol.argtypes = [VP, D, VP]
         L.cvls_port_set_matrix.restype = None
         L.cvls_port_set_matrix.argtypes = [VP, VP, VP]
+        L.cvls_port_set_fixed_point.restype = None
+        L.cvls_port_set_fixed_point.argtypes = [VP, I]
         L._cvls_declared = True
     return L
 
@@ -160,14 +168,16 @@ def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, threads=None,
-                       direct=False):
+                       direct=False, fixed_point=None):
     """The reference's CVode (BDF, Newton, SPGMR with left preconditioning and
     maxl 5, user J v and preconditioner) on the problem whose serial
     callbacks make_serial(L) builds (an object with .addresses() -> (f,
     jtimes, psetup, psolve) and .arr(N_Vector) -> numpy view).  atol: a
     scalar (CVodeSStolerances) or an array (CVodeSVtolerances).  direct:
     SUNDenseMatrix + SUNLINSOL_DENSE and the problem's .jac_address() instead
-    (the matrix-based path of CVLS)."""
+    (the matrix-based path of CVLS).  fixed_point = m: SUNNonlinSol_FixedPoint
+    with Anderson depth m and no linear solver (the linear-solver counters
+    are then 0)."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -186,8 +196,11 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
         prob.arr(vatol)[:] = atol
         assert L.CVodeSVtolerances(mem, rtol, vatol) == 0
     assert L.CVodeSetMaxNumSteps(mem, mxstep) == 0
-    A = None
-    if direct:
+    A, LS, NLS = None, None, None
+    if fixed_point is not None:
+        NLS = L.SUNNonlinSol_FixedPoint(y, fixed_point, ctx)
+        assert L.CVodeSetNonlinearSolver(mem, NLS) == 0
+    elif direct:
         A = L.SUNDenseMatrix(n, n, ctx)
         LS = L.SUNLinSol_Dense(y, A, ctx)
         assert L.CVodeSetLinearSolver(mem, LS, A) == 0
@@ -210,15 +223,20 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
                      "CVodeGetNumErrTestFails", "CVodeGetNumLinSolvSetups", "CVodeGetNumLinIters",
                      "CVodeGetNumPrecEvals", "CVodeGetNumPrecSolves", "CVodeGetNumJtimesEvals",
                      "CVodeGetNumLinConvFails"):
+            if NLS and name in LS_GETTERS:
+                row.append(0)
+                continue
             getattr(L, name)(mem, ct.byref(c))
             row.append(c.value)
         for name in ("CVodeGetLastOrder", "CVodeGetCurrentOrder"):
             getattr(L, name)(mem, ct.byref(li))
             row.append(li.value)
-        L.CVodeGetNumLinRhsEvals(mem, ct.byref(c))
-        row.append(c.value)
-        L.CVodeGetNumJacEvals(mem, ct.byref(c))
-        row.append(c.value)
+        for name in ("CVodeGetNumLinRhsEvals", "CVodeGetNumJacEvals"):
+            if NLS:
+                row.append(0)
+                continue
+            getattr(L, name)(mem, ct.byref(c))
+            row.append(c.value)
         rrow = []
         for name in ("CVodeGetLastStep", "CVodeGetCurrentStep", "CVodeGetCurrentTime",
                      "CVodeGetActualInitStep"):
@@ -229,7 +247,10 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
         sols.append(prob.arr(y).copy())
     pm = VP(mem)
     L.CVodeFree(ct.byref(pm))
-    L.SUNLinSolFree(LS)
+    if LS:
+        L.SUNLinSolFree(LS)
+    if NLS:
+        L.SUNNonlinSolFree(NLS)
     if A:
         L.SUNMatDestroy(A)
     L.N_VDestroy(y)
@@ -240,14 +261,16 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
-             vatol_handle=None, matrix=None):
+             vatol_handle=None, matrix=None, fixed_point=None):
     """The restated CVODE on whatever objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (f, jtimes, psetup, psolve,
     user_data) addresses, get(handle) -> numpy copy of a vector;
     vatol_handle: an N_Vector of absolute tolerances (else atol, a scalar);
     matrix = (SUNMatrix, CVLsJacFn address): the matrix-based path with a
-    direct LS_handle (callbacks then only need f and the user data)."""
+    direct LS_handle (callbacks then only need f and the user data);
+    fixed_point = m: the fixed-point solver with Anderson depth m and no
+    linear solver (LS_handle None)."""
     P = port_lib()
     f, jt, ps, pv, data = callbacks
     mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, 0.0 if vatol_handle else atol, mxstep,
@@ -257,6 +280,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
         P.cvls_port_set_vabstol(mem, rtol, vatol_handle)
     if matrix is not None:
         P.cvls_port_set_matrix(mem, matrix[0], matrix[1])
+    if fixed_point is not None:
+        P.cvls_port_set_fixed_point(mem, fixed_point)
     cnt, real, sols = [], [], []
     t = D()
     c = (ct.c_long * len(COUNTER_NAMES))()
@@ -280,7 +305,7 @@ def run_port_serial(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10):
                                 atol)
 
 
-def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False):
+def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False, fixed_point=None):
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -288,8 +313,10 @@ def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False):
     n = len(u0)
     y = L.N_VNew_Serial(n, ctx)
     prob.arr(y)[:] = u0
-    A, matrix = None, None
-    if direct:
+    A, matrix, LS = None, None, None
+    if fixed_point is not None:
+        cbs = (prob.addresses()[0], None, None, None, None)
+    elif direct:
         A = L.SUNDenseMatrix(n, n, ctx)
         LS = L.SUNLinSol_Dense(y, A, ctx)
         matrix = (A, prob.jac_address())
@@ -303,9 +330,10 @@ def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False):
         prob.arr(vatol)[:] = atol
     try:
         return run_port(y, LS, cbs, lambda h: prob.arr(h).copy(), touts, rtol, atol,
-                        vatol_handle=vatol, matrix=matrix)
+                        vatol_handle=vatol, matrix=matrix, fixed_point=fixed_point)
     finally:
-        L.SUNLinSolFree(LS)
+        if LS:
+            L.SUNLinSolFree(LS)
         if A:
             L.SUNMatDestroy(A)
         L.N_VDestroy(y)

@@ -16,9 +16,12 @@ difference-quotient J v and PSolve = the per-cell reaction solve; and
   solve as its linear solve and no SUNLinearSolver (the wrapper restated in
   oracle/arkstep.py around the reference's own SUNNonlinSol_Newton: the
   reference's build here has no MPI for the MPIPlusX vector it requires);
+* ``fpdirk_`` / ``fpimex_``: ARK-DIRK / ARK-IMEX with ``--nls fixedpoint``
+  (SUNNonlinSol_FixedPoint, Anderson depth 3, no linear solver), whose steps
+  the stiff reaction limits to ~1e-5: over ``--tf 0.01 --nout 2`` (their own
+  ``touts``);
 
-on the
-benchmark's defaults (rtol 1e-6, atol 1e-9, t in [0, 10], 10 outputs,
+on the benchmark's defaults (rtol 1e-6, atol 1e-9, t in [0, 10], 10 outputs,
 c = 0.01) on a 16^3 grid, with the user functions of
 oracle/bruss3d_cvode.py.  Stores u0, the Butcher tables each run used (read
 from the reference's table objects), the counters after every output
@@ -50,14 +53,21 @@ def main():
     out = {"grid": np.array([NPTS] * 3), "touts": np.array(q.touts),
            "tol": np.array([q.rtol, q.atol]), "u0": bc.initial(q),
            "omp_threads": np.array(THREADS)}
-    for name, imex, tl in (("dirk_", False, False), ("imex_", True, False), ("tl_", True, True)):
-        c, r, s, tables = bc.run_reference_arkode(q, imex=imex, task_local=tl)
+    qfp = bc.Params(NPTS, NPTS, NPTS, tf=0.01, nout=2)
+    for name, imex, tl, fp in (("dirk_", False, False, None), ("imex_", True, False, None),
+                               ("tl_", True, True, None), ("fpdirk_", False, False, 3),
+                               ("fpimex_", True, False, 3)):
+        qq = qfp if fp else q
+        if fp:
+            out[name + "touts"] = np.array(qq.touts)
+        c, r, s, tables = bc.run_reference_arkode(qq, imex=imex, task_local=tl, fixed_point=fp)
         out.update({name + "counters": c, name + "reals": r, name + "y_last": s[-1],
                     **ak.tables_to_dict(tables, name)})
         print(name, dict(zip(ak.COUNTER_NAMES, c[-1].tolist())))
         oc, ow = [], []
         for th in THREADS:
-            c2, _, s2, _ = bc.run_reference_arkode(q, threads=th, imex=imex, task_local=tl)
+            c2, _, s2, _ = bc.run_reference_arkode(qq, threads=th, imex=imex, task_local=tl,
+                                                   fixed_point=fp)
             w = 1.0 / (q.rtol * np.abs(s) + q.atol)
             oc.append(c2[-1])
             ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))

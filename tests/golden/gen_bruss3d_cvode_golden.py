@@ -10,7 +10,9 @@ oracle/bruss3d_cvode.py.  Stores u0 (its exp / pow are the host's), the
 counters after every output, hu / h / tn / h0u, the solution at the last
 output, and the same run on NVECTOR_OPENMP with 2, 3, 4, 6, 8 and 16 threads
 (a sample of the reference's own sensitivity to the summation order of its
-reductions).
+reductions).  The ``fp_`` entries are the same for the driver's
+``--nls fixedpoint`` variant (SUNNonlinSol_FixedPoint, Anderson depth
+``--fpaccel`` 3, no linear solver).
 
 Usage (where the reference sources exist):
     python -m sundials_gb300.build && python tests/golden/gen_bruss3d_cvode_golden.py
@@ -46,6 +48,19 @@ def main():
     out["omp_threads"] = np.array(THREADS)
     out["omp_counters"] = np.array(oc, np.int64)
     out["omp_wrms"] = np.array(ow)
+    c, r, s = bc.run_reference(q, fixed_point=3)
+    out.update({"fp_counters": c, "fp_reals": r, "fp_y_last": s[-1]})
+    print("fixed point:", dict(zip(hc.COUNTER_NAMES, c[-1].tolist())))
+    oc, ow = [], []
+    for th in THREADS:
+        c2, _, s2 = bc.run_reference(q, threads=th, fixed_point=3)
+        w = 1.0 / (q.rtol * np.abs(s) + q.atol)
+        oc.append(c2[-1])
+        ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))
+    out["fp_omp_counters"] = np.array(oc, np.int64)
+    out["fp_omp_wrms"] = np.array(ow)
+    print("  order sensitivity:", (np.array(oc) - c[-1]).min(axis=0).tolist(),
+          (np.array(oc) - c[-1]).max(axis=0).tolist(), "wrms", max(ow))
     print("order sensitivity:", {n: (int(np.min(np.array(oc)[:, k] - c[-1][k])),
                                      int(np.max(np.array(oc)[:, k] - c[-1][k])))
                                  for k, n in enumerate(hc.COUNTER_NAMES)}, "wrms", max(ow))

@@ -59,3 +59,38 @@ def test_arkstep_bruss3d_matches_reference(name, fused, fma):
     yr = g[name + "y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
     assert w <= max(3.0 * float(g[name + "omp_wrms"].max()), 1e-6), w
+
+
+@pytest.mark.parametrize("name", ["fpdirk_", "fpimex_"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_arkstep_bruss3d_fixed_point_matches_reference(name, fma):
+    """ARK-DIRK / ARK-IMEX with ``--nls fixedpoint`` (Anderson depth 3, no
+    linear solver) over t in [0, 0.01] on the 16^3 grid: hundreds of steps
+    and of nonlinear failures, which the reference's own summation order
+    already moves (its NVECTOR_OPENMP runs), so each counter must lie within
+    the reference's own largest deviation + 1 (equal where it never moved)
+    and the last solution within 3x its own weighted RMS deviation."""
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    g = np.load(GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    tables = ak.tables_from(g, name)
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        fe, fi, _, _, data = P.arkode_callbacks(imex=tables["e"] is not None)
+        c, r, s = ak.run_port(y.v, None, (fe, fi, None, None, data), lambda h: y.get(),
+                              [float(t) for t in g[name + "touts"]], tables, rtol, atol,
+                              fixed_point=3)
+    finally:
+        P.free()
+    ref = g[name + "counters"][-1]
+    own = np.abs(g[name + "omp_counters"] - ref).max(axis=0)
+    band = np.where(own == 0, 0, own + 1)
+    dev = np.abs(c[-1] - ref)
+    assert np.all(dev <= band), {n: (int(d), int(b)) for n, d, b in zip(ak.COUNTER_NAMES, dev, band)
+                                 if d > b}
+    yr = g[name + "y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g[name + "omp_wrms"].max()), 1e-6), w

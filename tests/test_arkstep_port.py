@@ -2,7 +2,8 @@
 reference's own ARKodeEvolve, both on the reference's NVECTOR_SERIAL and
 SUNLINSOL_SPGMR, on the 3-D advection-reaction benchmark's ARK-DIRK and
 ARK-IMEX configurations (arkode_driver.cpp:51-160, 239-370) at orders 2-4 and
-on ARK-IMEX with its task-local Newton (546-780, one task), with the
+on ARK-IMEX with its task-local Newton (546-780, one task), and on both with
+``--nls fixedpoint`` (SUNNonlinSol_FixedPoint, Anderson depth 3), with the
 benchmark's user functions restated in oracle/bruss3d_cvode.py:
 every counter, step size and solution value after every output time must be
 identical, bit for bit."""
@@ -78,6 +79,48 @@ def test_port_reproduces_golden(name):
     q = bc.Params(*(int(v) for v in g["grid"]))
     assert np.array_equal(bc.initial(q), g["u0"])
     c, r, s = bc.run_port_serial_arkode(q, ak.tables_from(g, name), task_local=name == "tl_")
+    assert np.array_equal(c, g[name + "counters"])
+    assert np.array_equal(r.view(np.int64), g[name + "reals"].view(np.int64))
+    assert np.array_equal(s[-1].view(np.int64), g[name + "y_last"].view(np.int64))
+
+
+@pytest.mark.parametrize("name", ["fpdirk_", "fpimex_"])
+def test_fixed_point_golden_layout(name):
+    g = np.load(GOLDEN)
+    assert len(g[name + "touts"]) == 2 and g[name + "touts"][-1] == 0.01
+    assert g[name + "counters"].shape == (2, len(ak.COUNTER_NAMES))
+    last = dict(zip(ak.COUNTER_NAMES, g[name + "counters"][-1]))
+    # the stiff reaction makes the iteration fail often; no linear solver
+    assert last["nni"] > 0 and last["nnf"] > 0 and last["nli"] == last["nps"] == 0
+    assert (ak.tables_from(g, name)["e"] is None) == (name == "fpdirk_")
+
+
+@needs_ref
+@pytest.mark.parametrize("imex", [False, True], ids=["dirk", "imex"])
+@pytest.mark.parametrize("shape,c,order", [((6, 5, 7), 0.01, 3), ((6, 5, 7), -0.02, 4),
+                                           ((5, 6, 4), 0.01, 2)])
+def test_fixed_point_bit_identical_to_reference(shape, c, order, imex):
+    """The fixed-point solver (oracle/fixedpoint_port.c) inside the ARKStep
+    restatement, over t in [0, 0.01] (hundreds of steps and of nonlinear
+    failures: the reaction is stiff)."""
+    q = bc.Params(*shape, c=c, tf=0.01, nout=2)
+    u0 = bc.initial(q)
+    c_ref, r_ref, s_ref, tables = ak.run_reference_with(lambda L: bc.SerialBruss(L, q), u0,
+                                                        q.touts, q.rtol, q.atol, order=order,
+                                                        imex=imex, fixed_point=3)
+    c_p, r_p, s_p = ak.run_port_serial_with(lambda L: bc.SerialBruss(L, q), u0, q.touts, tables,
+                                            q.rtol, q.atol, fixed_point=3)
+    assert np.array_equal(c_p, c_ref), (c_p[-1] - c_ref[-1]).tolist()
+    assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
+    assert np.array_equal(s_p.view(np.int64), s_ref.view(np.int64))
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["fpdirk_", "fpimex_"])
+def test_fixed_point_golden_reproduced(name):
+    g = np.load(GOLDEN)
+    q = bc.Params(*(int(v) for v in g["grid"]), tf=0.01, nout=2)
+    c, r, s = bc.run_port_serial_arkode(q, ak.tables_from(g, name), fixed_point=3)
     assert np.array_equal(c, g[name + "counters"])
     assert np.array_equal(r.view(np.int64), g[name + "reals"].view(np.int64))
     assert np.array_equal(s[-1].view(np.int64), g[name + "y_last"].view(np.int64))

@@ -60,3 +60,38 @@ def test_golden_is_the_reference_today():
     assert np.array_equal(c, g["counters"]) and np.array_equal(c2, c)
     assert np.array_equal(s[-1].view(np.int64), g["y_last"].view(np.int64))
     assert np.array_equal(s2.view(np.int64), s.view(np.int64))
+
+
+@needs_ref
+@pytest.mark.parametrize("shape,c", [((6, 5, 7), 0.01), ((8, 8, 8), -0.02)])
+def test_fixed_point_restatement_is_the_reference_cvode(shape, c):
+    """cvode_driver.cpp's ``--nls fixedpoint`` variant (SUNNonlinSol_FixedPoint,
+    Anderson depth 3, no linear solver): the restatement
+    (oracle/fixedpoint_port.c inside oracle/cvode_ls_port.c) bit for bit."""
+    q = bc.Params(*shape, c=c)
+    c_ref, r_ref, y_ref = bc.run_reference(q, fixed_point=3)
+    c_p, r_p, y_p = bc.run_port_serial(q, fixed_point=3)
+    assert np.array_equal(c_p, c_ref)
+    assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
+    assert np.array_equal(y_p.view(np.int64), y_ref.view(np.int64))
+    last = dict(zip(hc.COUNTER_NAMES, c_ref[-1]))
+    assert last["nni"] > 0 and last["nli"] == 0  # fixed point, no linear solver
+
+
+def test_fixed_point_golden_layout():
+    g = np.load(GOLDEN)
+    assert g["fp_counters"].shape == g["counters"].shape
+    assert g["fp_y_last"].shape == g["y_last"].shape
+    assert g["fp_omp_counters"].shape == g["omp_counters"].shape
+    last = dict(zip(hc.COUNTER_NAMES, g["fp_counters"][-1]))
+    assert last["nni"] > 0 and last["nli"] == last["nps"] == last["nsetups"] == 0
+
+
+@needs_ref
+def test_fixed_point_golden_reproduced():
+    g = np.load(GOLDEN)
+    q = bc.Params(*(int(v) for v in g["grid"]))
+    c, r, s = bc.run_port_serial(q, fixed_point=3)
+    assert np.array_equal(c, g["fp_counters"])
+    assert np.array_equal(r.view(np.int64), g["fp_reals"].view(np.int64))
+    assert np.array_equal(s[-1].view(np.int64), g["fp_y_last"].view(np.int64))

@@ -245,3 +245,37 @@ def test_cvode_bruss3d_matches_reference(fused, fma):
     yr = g["y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
     assert w <= max(3.0 * float(g["omp_wrms"].max()), 1e-6), w
+
+
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_cvode_bruss3d_fixed_point_matches_reference(fma):
+    """cvode_driver.cpp's ``--nls fixedpoint`` variant (Anderson depth 3, no
+    linear solver: every operation is an NVECTOR_GB300 one, the fused dot
+    products included) on the 16^3 grid to t = 10.  Here the reference is
+    sensitive to its own summation order (its NVECTOR_OPENMP runs move steps
+    and iterations by up to a few hundred and the solution by many
+    tolerances), so the bar is the band logic: each counter within the
+    reference's own largest deviation + 1 (equal where it never moved), the
+    last solution within 3x its own weighted RMS deviation."""
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    g = np.load(BR_GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        f, _, _, _, data = P.cvode_callbacks()
+        c, r, s = hc.run_port(y.v, None, (f, None, None, None, data), lambda h: y.get(),
+                              [float(t) for t in g["touts"]], rtol, atol, fixed_point=3)
+    finally:
+        P.free()
+    ref = g["fp_counters"][-1]
+    own = np.abs(g["fp_omp_counters"] - ref).max(axis=0)
+    band = np.where(own == 0, 0, own + 1)
+    dev = np.abs(c[-1] - ref)
+    assert np.all(dev <= band), {n: (int(d), int(b)) for n, d, b in zip(hc.COUNTER_NAMES, dev, band)
+                                 if d > b}
+    yr = g["fp_y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g["fp_omp_wrms"].max()), 1e-6), w
