@@ -201,16 +201,17 @@ class SerialBruss:
         return tuple(hc.ct.cast(c, hc.VP).value for c in self.cbs[2:4])
 
 
-def run_reference(q: Params, threads=None, fixed_point=None):
+def run_reference(q: Params, threads=None, fixed_point=None, adams=False):
     """cvode_driver.cpp's CV-BDF configuration through the reference's CVode
-    (fixed_point = m: ``--nls fixedpoint --fpaccel m``)."""
+    (fixed_point = m: ``--nls fixedpoint --fpaccel m``; adams: its CV-ADAMS
+    configuration, which always takes the fixed-point solver)."""
     return hc.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol,
-                                 q.atol, threads=threads, fixed_point=fixed_point)
+                                 q.atol, threads=threads, fixed_point=fixed_point, adams=adams)
 
 
-def run_port_serial(q: Params, fixed_point=None):
+def run_port_serial(q: Params, fixed_point=None, adams=False):
     return hc.run_port_serial_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol,
-                                   q.atol, fixed_point=fixed_point)
+                                   q.atol, fixed_point=fixed_point, adams=adams)
 
 
 def run_reference_arkode(q: Params, threads=None, imex=False, order=3, task_local=False,

@@ -4,7 +4,8 @@
  * iterative SUNLinearSolver (user or difference-quotient Jacobian-times-
  * vector, optional preconditioner) or a matrix-based direct one (SUNMatrix,
  * user Jacobian) -- or the fixed-point nonlinear solver with Anderson
- * acceleration and no linear solver (oracle/fixedpoint_port.c) -- restated
+ * acceleration and no linear solver (oracle/fixedpoint_port.c), with BDF or
+ * (CV_ADAMS) Adams-Moulton -- restated
  * over the generic object model: every vector operation is dispatched through
  * the vector's ops table the way the reference's generic layer dispatches it
  * (fused and vector-array operations when the vector provides them, the
@@ -21,6 +22,8 @@
  *   cvEwtSetSS / cvEwtSetSV        cvode.c:4791-4860
  *   cvHin / cvUpperBoundH0 / cvYddNorm   cvode.c:2161-2340
  *   cvStep and its callees         cvode.c:2367-3727
+ *   (Adams: cvAdjustAdams, cvSetAdams, cvAdamsStart, cvAdamsFinish, cvAltSum
+ *                                  cvode.c:2545-2600, 2800-2940)
  *   CVodeGetDky (k = 0)            cvode.c:1671-1750
  *   cvNlsResidual / LSetup / LSolve / ConvTest / FPFunction
  *                                  src/cvode/cvode_nls.c:256-425
@@ -39,7 +42,8 @@
 #include "../include/sundials_gb300_abi.h"
 #include "fixedpoint_port.h"
 
-#define QMAX 5
+#define QMAX 5      /* BDF_Q_MAX */
+#define QMAX_ALL 12 /* ADAMS_Q_MAX: array sizes */
 #define UROUND DBL_EPSILON
 
 /* CVODE / CVLS / Newton defaults (cvode_impl.h:55-127, cvode.c:118-125,
@@ -109,7 +113,7 @@ typedef struct
   SUNMatrix A, savedJ; /* matrix-based (direct) solver: A and CVLS's saved J */
   CvlsJacFn jac;
   /* vectors */
-  N_Vector zn[QMAX + 1], ewt, acor, tempv, ftemp, y, delta, ls_x, ls_ytemp;
+  N_Vector zn[QMAX_ALL + 1], ewt, acor, tempv, ftemp, y, delta, ls_x, ls_ytemp;
   N_Vector vtemp1, vtemp2, vtemp3;
   N_Vector ycur, fcur; /* CVLS's pointers to the current state and RHS */
   N_Vector Vabstol;    /* CVodeSVtolerances' copy, or NULL for scalar atol */
@@ -126,7 +130,8 @@ typedef struct
   /* integrator */
   double tn, h, hscale, hprime, next_h, eta, etamax, etaq, etaqm1, etaqp1, hu, h0u, saved_tq5;
   double rl1, gamma, gammap, gamrat, crate, delp, acnrm;
-  double tq[6], l[QMAX + 2], tau[QMAX + 2], cvals[QMAX + 1];
+  double tq[6], l[QMAX_ALL + 2], tau[QMAX_ALL + 2], cvals[QMAX_ALL + 1];
+  int qmax, adams; /* CV_ADAMS (qmax 12) or CV_BDF (qmax 5) */
   int q, qprime, qwait, L, indx_acor, nscon, convfail, qu, next_q;
   sunbooleantype cv_jcur;
   long nst, nfe, nsetups, nni, ncfn, netf, nnf, nstlp;
@@ -474,7 +479,7 @@ static void rescale(CvlsPort* m)
 static void increase_bdf(CvlsPort* m)
 {
   double alpha0, alpha1, prod, xi, xiold, hsum, A1;
-  for (int i = 0; i <= QMAX; i++) m->l[i] = 0.0;
+  for (int i = 0; i <= m->qmax; i++) m->l[i] = 0.0;
   m->l[2] = alpha1 = prod = xiold = 1.0;
   alpha0                          = -1.0;
   hsum                            = m->hscale;
@@ -497,7 +502,7 @@ static void increase_bdf(CvlsPort* m)
 static void decrease_bdf(CvlsPort* m)
 {
   double hsum, xi;
-  for (int i = 0; i <= QMAX; i++) m->l[i] = 0.0;
+  for (int i = 0; i <= m->qmax; i++) m->l[i] = 0.0;
   m->l[2] = 1.0;
   hsum    = 0.0;
   for (int j = 1; j <= m->q - 2; j++)
@@ -510,10 +515,34 @@ static void decrease_bdf(CvlsPort* m)
   if (m->q > 2) v_scaleaddmulti(m->q - 2, m->cvals, m->zn[m->q], m->zn + 2, m->zn + 2);
 }
 
+/* cvAdjustAdams (cvode.c:2550-2600): a new zero column on an increase; on
+ * a decrease each zn[j] loses a multiple of zn[q] */
+static void adjust_adams(CvlsPort* m, int deltaq)
+{
+  if (deltaq == 1)
+  {
+    v_const(0.0, m->zn[m->L]);
+    return;
+  }
+  double xi, hsum = 0.0;
+  for (int i = 0; i <= m->qmax; i++) m->l[i] = 0.0;
+  m->l[1] = 1.0;
+  for (int j = 1; j <= m->q - 2; j++)
+  {
+    hsum += m->tau[j];
+    xi = hsum / m->hscale;
+    for (int i = j + 1; i >= 1; i--) m->l[i] = m->l[i] * xi + m->l[i - 1];
+  }
+  for (int j = 1; j <= m->q - 2; j++) m->l[j + 1] = m->q * (m->l[j] / (j + 1));
+  for (int j = 2; j < m->q; j++) m->cvals[j - 2] = -m->l[j];
+  if (m->q > 2) v_scaleaddmulti(m->q - 2, m->cvals, m->zn[m->q], m->zn + 2, m->zn + 2);
+}
+
 static void adjust_order(CvlsPort* m, int deltaq)
 {
   if ((m->q == 2) && (deltaq != 1)) return;
-  if (deltaq == 1) increase_bdf(m);
+  if (m->adams) adjust_adams(m, deltaq);
+  else if (deltaq == 1) increase_bdf(m);
   else if (deltaq == -1) decrease_bdf(m);
 }
 
@@ -598,9 +627,68 @@ static void set_bdf(CvlsPort* m)
   set_tq_bdf(m, hsum, alpha0, alpha0_hat, xi_inv, xistar_inv);
 }
 
+/* cvAltSum: sum_{i=0}^{iend} (-1)^i a[i] / (i + k) */
+static double alt_sum(int iend, const double* a, int k)
+{
+  if (iend < 0) return 0.0;
+  double sum = 0.0;
+  int sign   = 1;
+  for (int i = 0; i <= iend; i++)
+  {
+    sum += sign * (a[i] / (i + k));
+    sign = -sign;
+  }
+  return sum;
+}
+
+/* cvSetAdams / cvAdamsStart / cvAdamsFinish (cvode.c:2815-2940) */
+static void set_adams(CvlsPort* m)
+{
+  double mm[QMAX_ALL + 1], M[3], hsum, xi_inv, sum;
+  if (m->q == 1)
+  {
+    m->l[0] = m->l[1] = m->tq[1] = m->tq[5] = 1.0;
+    m->tq[2] = 0.5;
+    m->tq[3] = 1.0 / 12.0;
+    m->tq[4] = CORTES / m->tq[2];
+    return;
+  }
+  hsum  = m->h;
+  mm[0] = 1.0;
+  for (int i = 1; i <= m->q; i++) mm[i] = 0.0;
+  for (int j = 1; j < m->q; j++)
+  {
+    if ((j == m->q - 1) && (m->qwait == 1))
+    {
+      sum      = alt_sum(m->q - 2, mm, 2);
+      m->tq[1] = m->q * sum / mm[m->q - 2];
+    }
+    xi_inv = m->h / hsum;
+    for (int i = j; i >= 1; i--) mm[i] += mm[i - 1] * xi_inv;
+    hsum += m->tau[j];
+  }
+  M[0] = alt_sum(m->q - 1, mm, 1);
+  M[1] = alt_sum(m->q - 1, mm, 2);
+  const double M0_inv = 1.0 / M[0];
+  m->l[0]             = 1.0;
+  for (int i = 1; i <= m->q; i++) m->l[i] = M0_inv * (mm[i - 1] / i);
+  const double xi = hsum / m->h;
+  xi_inv          = 1.0 / xi;
+  m->tq[2]        = M[1] * M0_inv / xi;
+  m->tq[5]        = xi / m->l[m->q];
+  if (m->qwait == 1)
+  {
+    for (int i = m->q; i >= 1; i--) mm[i] += mm[i - 1] * xi_inv;
+    M[2]     = alt_sum(m->q, mm, 2);
+    m->tq[3] = M[2] * M0_inv / m->L;
+  }
+  m->tq[4] = CORTES / m->tq[2];
+}
+
 static void set_coeffs(CvlsPort* m)
 {
-  set_bdf(m);
+  if (m->adams) set_adams(m);
+  else set_bdf(m);
   m->rl1   = 1.0 / m->l[1];
   m->gamma = m->h * m->rl1;
   if (m->nst == 0) m->gammap = m->gamma;
@@ -729,11 +817,11 @@ static void complete_step(CvlsPort* m)
   m->tau[1] = m->h;
   v_scaleaddmulti(m->q + 1, m->l, m->acor, m->zn, m->zn);
   m->qwait--;
-  if ((m->qwait == 1) && (m->q != QMAX))
+  if ((m->qwait == 1) && (m->q != m->qmax))
   {
-    v_scale(1.0, m->acor, m->zn[QMAX]);
+    v_scale(1.0, m->acor, m->zn[m->qmax]);
     m->saved_tq5 = m->tq[5];
-    m->indx_acor = QMAX;
+    m->indx_acor = m->qmax;
   }
 }
 
@@ -775,13 +863,13 @@ static double compute_etaqm1(CvlsPort* m)
 static double compute_etaqp1(CvlsPort* m)
 {
   m->etaqp1 = 0.0;
-  if (m->q != QMAX)
+  if (m->q != m->qmax)
   {
     if (m->saved_tq5 == 0.0) return m->etaqp1;
     double base = m->h / m->tau[2], p = 1.0;
     for (int i = 1; i <= m->L; i++) p *= base; /* SUNRpowerI */
     double cquot = (m->tq[5] / m->saved_tq5) * p;
-    v_linearsum(-cquot, m->zn[QMAX], 1.0, m->acor, m->tempv);
+    v_linearsum(-cquot, m->zn[m->qmax], 1.0, m->acor, m->tempv);
     double dup = v_wrms(m->tempv, m->ewt) * m->tq[3];
     m->etaqp1  = 1.0 / (pow(BIAS3 * dup, 1.0 / (m->L + 1)) + ADDON);
   }
@@ -812,7 +900,7 @@ static void choose_eta(CvlsPort* m)
   {
     m->eta    = m->etaqp1;
     m->qprime = m->q + 1;
-    v_scale(1.0, m->acor, m->zn[QMAX]);
+    if (!m->adams) v_scale(1.0, m->acor, m->zn[m->qmax]);
   }
 }
 
@@ -962,7 +1050,7 @@ static int get_dky(CvlsPort* m, double t, N_Vector dky)
   double tp = m->tn - m->hu - tfuzz, tn1 = m->tn + tfuzz;
   if ((t - tp) * (t - tn1) > 0.0) return CV_BAD_T;
   double s = (t - m->tn) / m->h;
-  N_Vector X[QMAX + 1] = {0};
+  N_Vector X[QMAX_ALL + 1] = {0};
   int nvec = 0;
   for (int j = m->q; j >= 0; j--)
   {
@@ -1013,6 +1101,7 @@ void* cvls_port_create(CvlsRhsFn f, double t0, N_Vector y0, double rtol, double 
   m->LS        = LS;
   m->tn        = t0;
   m->q         = 1;
+  m->qmax      = QMAX;
   m->L         = 2;
   m->qwait     = m->L;
   m->etamax    = ETA_MAX_FS;
@@ -1043,6 +1132,17 @@ void cvls_port_set_fixed_point(void* mem, int depth)
 {
   CvlsPort* m = (CvlsPort*)mem;
   m->fp       = fp_port_create(m->ewt, depth);
+}
+
+/* CVodeCreate(CV_ADAMS, ...) instead of CV_BDF: Adams-Moulton of orders 1-12
+ * (call before the first solve; the history array grows to 13 vectors). */
+void cvls_port_set_adams(void* mem)
+{
+  CvlsPort* m = (CvlsPort*)mem;
+  if (m->adams) return;
+  m->adams = 1;
+  m->qmax  = QMAX_ALL;
+  for (int j = QMAX + 1; j <= QMAX_ALL; j++) m->zn[j] = m->zn[0]->ops->nvclone(m->zn[0]);
 }
 
 /* CVodeSVtolerances(rtol, abstol): a copy of abstol is kept (all entries > 0). */
@@ -1159,7 +1259,7 @@ void cvls_port_free(void* mem)
   N_Vector vs[] = {m->ewt,   m->acor, m->tempv,  m->ftemp,  m->y,     m->delta,
                    m->ls_ytemp, m->ls_x, m->vtemp1, m->vtemp2, m->vtemp3};
   for (int i = 0; i < (int)(sizeof(vs) / sizeof(vs[0])); i++) vs[i]->ops->nvdestroy(vs[i]);
-  for (int j = 0; j <= QMAX; j++) m->zn[j]->ops->nvdestroy(m->zn[j]);
+  for (int j = 0; j <= m->qmax; j++) m->zn[j]->ops->nvdestroy(m->zn[j]);
   if (m->Vabstol) m->Vabstol->ops->nvdestroy(m->Vabstol);
   if (m->savedJ) m->savedJ->ops->destroy(m->savedJ);
   fp_port_free(m->fp);

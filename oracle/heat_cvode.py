@@ -117,6 +117,8 @@ def port_lib() -> ct.CDLL:
         L.cvls_port_set_matrix.argtypes = [VP, VP, VP]
         L.cvls_port_set_fixed_point.restype = None
         L.cvls_port_set_fixed_point.argtypes = [VP, I]
+        L.cvls_port_set_adams.restype = None
+        L.cvls_port_set_adams.argtypes = [VP]
         L._cvls_declared = True
     return L
 
@@ -168,7 +170,7 @@ def run_reference(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, threads=None,
-                       direct=False, fixed_point=None):
+                       direct=False, fixed_point=None, adams=False):
     """The reference's CVode (BDF, Newton, SPGMR with left preconditioning and
     maxl 5, user J v and preconditioner) on the problem whose serial
     callbacks make_serial(L) builds (an object with .addresses() -> (f,
@@ -177,7 +179,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
     SUNDenseMatrix + SUNLINSOL_DENSE and the problem's .jac_address() instead
     (the matrix-based path of CVLS).  fixed_point = m: SUNNonlinSol_FixedPoint
     with Anderson depth m and no linear solver (the linear-solver counters
-    are then 0)."""
+    are then 0).  adams: CVodeCreate(CV_ADAMS) instead of CV_BDF."""
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -185,7 +187,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
     n = len(u0)
     y = L.N_VNew_Serial(n, ctx) if threads is None else L.N_VNew_OpenMP(n, threads, ctx)
     prob.arr(y)[:] = u0
-    mem = L.CVodeCreate(2, ctx)
+    mem = L.CVodeCreate(1 if adams else 2, ctx)
     f, jt, ps, pv = prob.addresses()
     assert L.CVodeInit(mem, f, 0.0, y) == 0
     vatol = None
@@ -261,7 +263,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, mxstep=100000, thread
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10, mxstep=100000,
-             vatol_handle=None, matrix=None, fixed_point=None):
+             vatol_handle=None, matrix=None, fixed_point=None, adams=False):
     """The restated CVODE on whatever objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (f, jtimes, psetup, psolve,
@@ -270,7 +272,7 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
     matrix = (SUNMatrix, CVLsJacFn address): the matrix-based path with a
     direct LS_handle (callbacks then only need f and the user data);
     fixed_point = m: the fixed-point solver with Anderson depth m and no
-    linear solver (LS_handle None)."""
+    linear solver (LS_handle None); adams: Adams-Moulton instead of BDF."""
     P = port_lib()
     f, jt, ps, pv, data = callbacks
     mem = P.cvls_port_create(f, 0.0, y0_handle, rtol, 0.0 if vatol_handle else atol, mxstep,
@@ -282,6 +284,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, rtol=1e-6, atol=1e-10,
         P.cvls_port_set_matrix(mem, matrix[0], matrix[1])
     if fixed_point is not None:
         P.cvls_port_set_fixed_point(mem, fixed_point)
+    if adams:
+        P.cvls_port_set_adams(mem)
     cnt, real, sols = [], [], []
     t = D()
     c = (ct.c_long * len(COUNTER_NAMES))()
@@ -305,7 +309,8 @@ def run_port_serial(nx: int, ny: int, touts, rtol=1e-6, atol=1e-10):
                                 atol)
 
 
-def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False, fixed_point=None):
+def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False, fixed_point=None,
+                         adams=False):
     L = ref_lib()
     ctx = VP()
     assert L.SUNContext_Create(0, ct.byref(ctx)) == 0
@@ -330,7 +335,8 @@ def run_port_serial_with(make_serial, u0, touts, rtol, atol, direct=False, fixed
         prob.arr(vatol)[:] = atol
     try:
         return run_port(y, LS, cbs, lambda h: prob.arr(h).copy(), touts, rtol, atol,
-                        vatol_handle=vatol, matrix=matrix, fixed_point=fixed_point)
+                        vatol_handle=vatol, matrix=matrix, fixed_point=fixed_point,
+                        adams=adams)
     finally:
         if LS:
             L.SUNLinSolFree(LS)

@@ -12,7 +12,10 @@ output, and the same run on NVECTOR_OPENMP with 2, 3, 4, 6, 8 and 16 threads
 (a sample of the reference's own sensitivity to the summation order of its
 reductions).  The ``fp_`` entries are the same for the driver's
 ``--nls fixedpoint`` variant (SUNNonlinSol_FixedPoint, Anderson depth
-``--fpaccel`` 3, no linear solver).
+``--fpaccel`` 3, no linear solver), and the ``adams_`` entries those of its
+CV-ADAMS configuration (Adams-Moulton, always with that fixed-point solver),
+whose steps the stiff reaction holds near 5e-6: over ``--tf 0.01 --nout 2``
+(their own ``adams_touts``).
 
 Usage (where the reference sources exist):
     python -m sundials_gb300.build && python tests/golden/gen_bruss3d_cvode_golden.py
@@ -59,6 +62,21 @@ def main():
         ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))
     out["fp_omp_counters"] = np.array(oc, np.int64)
     out["fp_omp_wrms"] = np.array(ow)
+    print("  order sensitivity:", (np.array(oc) - c[-1]).min(axis=0).tolist(),
+          (np.array(oc) - c[-1]).max(axis=0).tolist(), "wrms", max(ow))
+    qa = bc.Params(NPTS, NPTS, NPTS, tf=0.01, nout=2)
+    c, r, s = bc.run_reference(qa, fixed_point=3, adams=True)
+    out.update({"adams_touts": np.array(qa.touts), "adams_counters": c, "adams_reals": r,
+                "adams_y_last": s[-1]})
+    print("adams:", dict(zip(hc.COUNTER_NAMES, c[-1].tolist())))
+    oc, ow = [], []
+    for th in THREADS:
+        c2, _, s2 = bc.run_reference(qa, threads=th, fixed_point=3, adams=True)
+        w = 1.0 / (qa.rtol * np.abs(s) + qa.atol)
+        oc.append(c2[-1])
+        ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))
+    out["adams_omp_counters"] = np.array(oc, np.int64)
+    out["adams_omp_wrms"] = np.array(ow)
     print("  order sensitivity:", (np.array(oc) - c[-1]).min(axis=0).tolist(),
           (np.array(oc) - c[-1]).max(axis=0).tolist(), "wrms", max(ow))
     print("order sensitivity:", {n: (int(np.min(np.array(oc)[:, k] - c[-1][k])),

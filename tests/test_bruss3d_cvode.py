@@ -95,3 +95,41 @@ def test_fixed_point_golden_reproduced():
     assert np.array_equal(c, g["fp_counters"])
     assert np.array_equal(r.view(np.int64), g["fp_reals"].view(np.int64))
     assert np.array_equal(s[-1].view(np.int64), g["fp_y_last"].view(np.int64))
+
+
+@needs_ref
+@pytest.mark.parametrize("shape,c,tf,k,rtol", [
+    ((6, 5, 7), -0.02, 0.01, None, 1e-6),                 # the benchmark's stiff reaction
+    ((6, 5, 7), -0.02, 10.0, (1, 1, 1, 1, 1, 1), 1e-10),  # non-stiff: orders up to 7
+    ((5, 6, 4), 0.02, 5.0, (1, 1, 1, 1, 2, 2), 1e-12)])
+def test_adams_restatement_is_the_reference_cvode(shape, c, tf, k, rtol):
+    """cvode_driver.cpp's CV-ADAMS configuration (Adams-Moulton with the
+    fixed-point solver): the restatement bit for bit, including orders above
+    BDF's 5 and order decreases (cvAdjustAdams)."""
+    kw = {} if k is None else {"k": k, "rtol": rtol, "atol": rtol * 1e-3}
+    q = bc.Params(*shape, c=c, tf=tf, nout=2 if k is None else 5, **kw)
+    c_ref, r_ref, y_ref = bc.run_reference(q, fixed_point=3, adams=True)
+    c_p, r_p, y_p = bc.run_port_serial(q, fixed_point=3, adams=True)
+    assert np.array_equal(c_p, c_ref)
+    assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
+    assert np.array_equal(y_p.view(np.int64), y_ref.view(np.int64))
+    if k is not None:
+        assert c_ref[:, list(hc.COUNTER_NAMES).index("qu")].max() > 5
+
+
+def test_adams_golden_layout():
+    g = np.load(GOLDEN)
+    assert len(g["adams_touts"]) == 2 and g["adams_touts"][-1] == 0.01
+    assert g["adams_counters"].shape == (2, len(hc.COUNTER_NAMES))
+    last = dict(zip(hc.COUNTER_NAMES, g["adams_counters"][-1]))
+    assert last["nst"] > 1000 and last["nli"] == 0
+
+
+@needs_ref
+def test_adams_golden_reproduced():
+    g = np.load(GOLDEN)
+    q = bc.Params(*(int(v) for v in g["grid"]), tf=0.01, nout=2)
+    c, r, s = bc.run_port_serial(q, fixed_point=3, adams=True)
+    assert np.array_equal(c, g["adams_counters"])
+    assert np.array_equal(r.view(np.int64), g["adams_reals"].view(np.int64))
+    assert np.array_equal(s[-1].view(np.int64), g["adams_y_last"].view(np.int64))

@@ -280,3 +280,38 @@ def test_cvode_bruss3d_fixed_point_matches_reference(fma):
     yr = g["fp_y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
     assert w <= max(3.0 * float(g["fp_omp_wrms"].max()), 1e-6), w
+
+
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_cvode_bruss3d_adams_matches_reference(fma):
+    """cvode_driver.cpp's CV-ADAMS configuration (Adams-Moulton with the
+    fixed-point solver, Anderson depth 3, no linear solver) on the 16^3 grid
+    over t in [0, 0.01] (some 3,200 steps: the stiff reaction bounds them).
+    The reference's own reduction-order runs never moved a counter here, so
+    every counter after every output must equal the reference's; the last
+    solution within 3x its own weighted RMS deviation or 1e-3 tolerances
+    (the own deviation is ~1e-6 here, below what one rounding per product
+    in the FMA mode moves over thousands of steps)."""
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    g = np.load(BR_GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        f, _, _, _, data = P.cvode_callbacks()
+        c, r, s = hc.run_port(y.v, None, (f, None, None, None, data), lambda h: y.get(),
+                              [float(t) for t in g["adams_touts"]], rtol, atol, fixed_point=3,
+                              adams=True)
+    finally:
+        P.free()
+    ref = g["adams_counters"]
+    own = np.abs(g["adams_omp_counters"] - ref[-1]).max(axis=0)
+    band = np.where(own == 0, 0, own + 1)
+    dev = np.abs(c[-1] - ref[-1])
+    assert np.all(dev <= band), {n: (int(d), int(b)) for n, d, b in zip(hc.COUNTER_NAMES, dev, band)
+                                 if d > b}
+    yr = g["adams_y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g["adams_omp_wrms"].max()), 1e-3), w
