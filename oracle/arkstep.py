@@ -30,17 +30,20 @@ TABLE_KEYS = ("A", "b", "c", "d", "orders")
 
 
 def tables_from(g, prefix=""):
-    """The tables dict of a fixture: keys <prefix>table_* (implicit) and
-    <prefix>etable_* (explicit, absent for a DIRK run)."""
+    """The tables dict of a fixture: keys <prefix>table_* (implicit, or the
+    ERK method's with <prefix>erk set) and <prefix>etable_* (explicit,
+    absent for a DIRK run)."""
     Ti = {k: g[prefix + "table_" + k] for k in TABLE_KEYS}
     Te = ({k: g[prefix + "etable_" + k] for k in TABLE_KEYS}
           if prefix + "etable_A" in g else None)
-    return {"i": Ti, "e": Te}
+    return {"i": Ti, "e": Te, "erk": bool(g[prefix + "erk"]) if prefix + "erk" in g else False}
 
 
 def tables_to_dict(tables, prefix=""):
     """Fixture entries of a tables dict (inverse of tables_from)."""
     out = {prefix + "table_" + k: v for k, v in tables["i"].items()}
+    if tables.get("erk"):
+        out[prefix + "erk"] = np.array(1)
     if tables["e"] is not None:
         out.update({prefix + "etable_" + k: v for k, v in tables["e"].items()})
     return out
@@ -78,6 +81,8 @@ def ref_lib() -> ct.CDLL:
                                              ct.POINTER(VP)]),
         ("SUNNonlinSolNewEmpty", VP, [VP]),
         ("SUNNonlinSol_FixedPoint", VP, [VP, I, VP]),
+        ("ERKStepCreate", VP, [VP, D, VP, VP]),
+        ("ERKStepGetCurrentButcherTable", I, [VP, ct.POINTER(ct.POINTER(_Table))]),
         ("SUNNonlinSolFreeEmpty", None, [VP]),
         ("SUNNonlinSolSetSysFn", I, [VP, VP]),
         ("SUNNonlinSolSetLSolveFn", I, [VP, VP]),
@@ -121,6 +126,8 @@ def port_lib() -> ct.CDLL:
         L.arkstep_port_set_task_local.argtypes = [VP, VP]
         L.arkstep_port_set_fixed_point.restype = None
         L.arkstep_port_set_fixed_point.argtypes = [VP, I]
+        L.arkstep_port_set_erk.restype = None
+        L.arkstep_port_set_erk.argtypes = [VP]
         L._arkstep_declared = True
     return L
 
@@ -229,7 +236,7 @@ def _read_table(T: _Table) -> dict:
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None,
-                       imex=False, task_local=False, fixed_point=None):
+                       imex=False, task_local=False, fixed_point=None, erk=False):
     """The reference's ARKodeEvolve on the problem whose serial callbacks
     make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
     psetup None, .imex_addresses() -> (fe, fi), and .arr(N_Vector)):
@@ -240,7 +247,9 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     problem's .reaction_into / .block_solve; the counters then end with its
     nonlinear-residual evaluations.  fixed_point = m: SUNNonlinSol_FixedPoint
     with Anderson depth m and no linear solver (``--nls fixedpoint``).
-    threads = k: NVECTOR_OPENMP on k threads
+    erk: the benchmark's ERK configuration (ERKStepCreate(f), no nonlinear
+    or linear solver; the method's table is returned as tables["i"] with
+    tables["erk"] set).  threads = k: NVECTOR_OPENMP on k threads
     instead of NVECTOR_SERIAL (its reductions sum in another order)."""
     L = ref_lib()
     ctx = VP()
@@ -252,14 +261,16 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     f, jt, ps, pv = prob.addresses()
     assert ps is None and jt is None
     fe, fi = prob.imex_addresses() if imex else (None, f)
-    mem = L.ARKStepCreate(fe, fi, 0.0, y, ctx)
+    mem = L.ERKStepCreate(f, 0.0, y, ctx) if erk else L.ARKStepCreate(fe, fi, 0.0, y, ctx)
     assert mem
     assert L.ARKodeSetOrder(mem, order) == 0
     assert L.ARKodeSStolerances(mem, rtol, atol) == 0
     assert L.ARKodeSetMaxNumSteps(mem, mxstep) == 0
-    TL, LS = None, None
-    no_ls = task_local or fixed_point is not None
-    if fixed_point is not None:
+    TL, LS, NLS = None, None, None
+    no_ls = task_local or fixed_point is not None or erk
+    if erk:
+        pass
+    elif fixed_point is not None:
         NLS = L.SUNNonlinSol_FixedPoint(y, fixed_point, ctx)
         assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
     elif task_local:
@@ -279,6 +290,10 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     for tout in touts:
         flag = L.ARKodeEvolve(mem, tout, y, ct.byref(t), 1)
         assert flag == 0, flag
+        if table is None and erk:
+            B = ct.POINTER(_Table)()
+            assert L.ERKStepGetCurrentButcherTable(mem, ct.byref(B)) == 0
+            table = {"i": _read_table(B.contents), "e": None, "erk": True}
         if table is None:
             Bi, Be = ct.POINTER(_Table)(), ct.POINTER(_Table)()
             assert L.ARKStepGetCurrentButcherTables(mem, ct.byref(Bi), ct.byref(Be)) == 0
@@ -289,13 +304,17 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         for name in ("ARKodeGetNumSteps", "ARKodeGetNumStepAttempts"):
             getattr(L, name)(mem, ct.byref(c))
             row.append(c.value)
-        L.ARKodeGetNumRhsEvals(mem, 1, ct.byref(c))
-        row.append(c.value)
+        if erk:
+            row.append(0)
+        else:
+            L.ARKodeGetNumRhsEvals(mem, 1, ct.byref(c))
+            row.append(c.value)
         for name in ("ARKodeGetNumErrTestFails", "ARKodeGetNumStepSolveFails",
                      "ARKodeGetNumNonlinSolvIters", "ARKodeGetNumNonlinSolvConvFails",
                      "ARKodeGetNumLinIters", "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals",
                      "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
-            if no_ls and any(k in name for k in ("Lin", "Prec", "Jtimes")):
+            if (no_ls and any(k in name for k in ("Lin", "Prec", "Jtimes"))
+                    or erk and "Nonlin" in name):
                 row.append(0)  # no linear solver attached
                 continue
             getattr(L, name)(mem, ct.byref(c))
@@ -315,7 +334,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     L.ARKodeFree(ct.byref(pm))
     if TL:
         TL.free()
-    else:
+    elif NLS:
         L.SUNNonlinSolFree(NLS)
     if LS:
         L.SUNLinSolFree(LS)
@@ -339,6 +358,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
     Ti, Te = tables["i"], tables["e"]
+    if tables.get("erk"):  # ERKStep: the single right-hand side goes in fi's place
+        fe, fi = None, fe or fi
     assert (fe is None) == (Te is None)
     keep = []
 
@@ -357,6 +378,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
         P.arkstep_port_set_task_local(mem, block_solve)
     if fixed_point is not None:
         P.arkstep_port_set_fixed_point(mem, fixed_point)
+    if tables.get("erk"):
+        P.arkstep_port_set_erk(mem)
     cnt, real, sols = [], [], []
     t = D()
     cbuf = (ct.c_long * len(COUNTER_NAMES))()
@@ -383,7 +406,7 @@ def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=
     prob = make_serial(L)
     y = L.N_VNew_Serial(len(u0), ctx)
     prob.arr(y)[:] = u0
-    no_ls = task_local or fixed_point is not None
+    no_ls = task_local or fixed_point is not None or tables.get("erk")
     LS = None if no_ls else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
     f, jt, _, pv = prob.addresses()
     fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)

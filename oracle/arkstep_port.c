@@ -5,8 +5,9 @@
  * solver and a matrix-free iterative SUNLinearSolver (user or
  * difference-quotient Jacobian-times-vector, a preconditioner solve without a
  * preconditioner setup), the benchmark's task-local Newton, or the
- * fixed-point solver with Anderson acceleration (oracle/fixedpoint_port.c) --
- * the ARK-DIRK and ARK-IMEX configurations of the
+ * fixed-point solver with Anderson acceleration (oracle/fixedpoint_port.c);
+ * and ERKStep (explicit only) -- the ERK, ARK-DIRK and ARK-IMEX
+ * configurations of the
  * 3-D advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
  * arkode_driver.cpp:51-160, 239-370) -- restated over the generic object model: every
  * vector operation is dispatched through the vector's ops table (fused
@@ -149,6 +150,10 @@ typedef struct
   long nli, nps, njtimes, nfeDQ, ncfl;
   /* I controller history (SUNAdaptController_UpdateH_Soderlind) */
   double c_ep, c_hp;
+  /* ERKStep instead of ARKStep: the method table is A/b/c/d, the right-hand
+   * side fi (counted in nfe); adaptivity safety and growth */
+  int erk;
+  double safety, growth;
 } ArkPort;
 
 /* ------------------------------------------------------ generic vector layer */
@@ -206,10 +211,48 @@ static void sum_first(ArkPort* m, N_Vector f)
   else v_scale(1.0, m->Fi[0], f);
 }
 
+/* erkStep_FullRHS (arkode_erkstep.c:591-735) */
+static int full_rhs_erk(ArkPort* m, double t, N_Vector y, N_Vector f, int mode)
+{
+  int r;
+  switch (mode)
+  {
+  case FULLRHS_START:
+    if (!m->fn_is_current)
+    {
+      r = m->fi(t, y, m->Fi[0], m->user_data);
+      m->nfe++;
+      if (r != 0) return ARK_RHSFUNC_FAIL;
+    }
+    v_scale(1.0, m->Fi[0], f);
+    break;
+  case FULLRHS_END:
+    if (!m->fn_is_current)
+    {
+      if (!m->sa_i)
+      {
+        r = m->fi(t, y, m->Fi[0], m->user_data);
+        m->nfe++;
+        if (r != 0) return ARK_RHSFUNC_FAIL;
+      }
+      else v_scale(1.0, m->Fi[m->s - 1], m->Fi[0]);
+      v_scale(1.0, m->Fi[0], f);
+    }
+    break;
+  default:
+    r = m->fi(t, y, f, m->user_data);
+    m->nfe++;
+    if (r != 0) return ARK_RHSFUNC_FAIL;
+    break;
+  }
+  return 0;
+}
+
 /* arkStep_FullRHS, identity mass matrix */
 static int full_rhs(ArkPort* m, double t, N_Vector y, N_Vector f, int mode)
 {
   int r;
+  if (m->erk) return full_rhs_erk(m, t, y, f, mode);
   switch (mode)
   {
   case FULLRHS_START:
@@ -552,8 +595,66 @@ static int compute_solutions(ArkPort* m, double* dsm)
   return 0;
 }
 
+/* erkStep_TakeStep / erkStep_ComputeSolutions (arkode_erkstep.c:736-997,
+ * 1413-1516): stage z_i = sum_j h A_ij F_j + yn in one linear combination,
+ * y = sum_j h b_j F_j + yn, error = sum_j h (b_j - d_j) F_j */
+static int take_step_erk(ArkPort* m, double* dsm, int* nflag)
+{
+  double cvals[MAXS + 1];
+  N_Vector X[MAXS + 1];
+  int nvec;
+  *nflag = ARK_SUCCESS;
+  if (!m->fn_is_current)
+  {
+    int r = full_rhs(m, m->tn, m->yn, m->fn, m->initsetup ? FULLRHS_START : FULLRHS_END);
+    if (r) return ARK_RHSFUNC_FAIL;
+    m->fn_is_current = SUNTRUE;
+  }
+  for (int is = 1; is < m->s; is++)
+  {
+    m->tcur = m->tn + m->c[is] * m->h;
+    nvec    = 0;
+    for (int js = 0; js < is; js++)
+    {
+      cvals[nvec] = m->h * m->A[is][js];
+      X[nvec]     = m->Fi[js];
+      nvec++;
+    }
+    cvals[nvec] = 1.0;
+    X[nvec]     = m->yn;
+    nvec++;
+    v_lincomb(nvec, cvals, X, m->ycur);
+    int r = m->fi(m->tcur, m->ycur, m->Fi[is], m->user_data);
+    m->nfe++;
+    if (r < 0) return ARK_RHSFUNC_FAIL;
+    if (r > 0) return ARK_UNREC_RHSFUNC_ERR;
+  }
+  nvec = 0;
+  for (int j = 0; j < m->s; j++)
+  {
+    cvals[nvec] = m->h * m->b[j];
+    X[nvec]     = m->Fi[j];
+    nvec++;
+  }
+  cvals[nvec] = 1.0;
+  X[nvec]     = m->yn;
+  nvec++;
+  v_lincomb(nvec, cvals, X, m->ycur);
+  nvec = 0;
+  for (int j = 0; j < m->s; j++)
+  {
+    cvals[nvec] = m->h * (m->b[j] - m->d[j]);
+    X[nvec]     = m->Fi[j];
+    nvec++;
+  }
+  v_lincomb(nvec, cvals, X, m->tempv1);
+  *dsm = v_wrms(m->tempv1, m->ewt);
+  return ARK_SUCCESS;
+}
+
 static int take_step(ArkPort* m, double* dsm, int* nflag)
 { /* arkStep_TakeStep_Z */
+  if (m->erk) return take_step_erk(m, dsm, nflag);
   int implicit_stage = fabs(m->A[0][0]) > TINY;
   const int is_start = implicit_stage ? 0 : 1;
   /* the Hermite module needs fn, so it is always evaluated (or copied) */
@@ -623,7 +724,7 @@ static void adapt(ArkPort* m, double hcur, double dsm)
   const double e1 = 1.0 * dsm;
   const double k1 = -1.0 / ord;
   double h_acc    = hcur * pow(e1, k1);
-  h_acc *= SAFETY;
+  h_acc *= m->safety;
   h_acc = dmin(fabs(h_acc), fabs(m->etamax * hcur));
   h_acc = dmax(h_acc, fabs(ETAMIN * hcur));
   if (dsm <= 1.0)
@@ -677,7 +778,7 @@ static int complete_step(ArkPort* m, double dsm)
   m->hold       = m->h;
   m->tn         = m->tcur;
   m->hprime     = m->h * m->eta;
-  m->etamax     = GROWTH;
+  m->etamax     = m->growth;
   m->initsetup  = SUNFALSE;
   m->firststage = SUNFALSE;
   return ARK_SUCCESS;
@@ -922,6 +1023,8 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
   m->eplifac    = ARKLS_EPLIN;
   m->nrmfac     = sqrt((double)y0->ops->nvgetlength(y0));
   m->c_ep = m->c_hp = 1.0;
+  m->safety = SAFETY;
+  m->growth = GROWTH;
   if (LS && LS->ops->setatimes) LS->ops->setatimes(LS, m, ls_atimes);
   if (LS && psolve && LS->ops->setpreconditioner)
     LS->ops->setpreconditioner(LS, m, NULL, ls_psolve);
@@ -934,6 +1037,18 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
 void arkstep_port_set_task_local(void* mem, ArkBlockSolveFn block_lsolve)
 {
   ((ArkPort*)mem)->block_lsolve = block_lsolve;
+}
+
+/* ERKStepCreate(f, ...) instead of ARKStepCreate: create with fe NULL, fi = f
+ * and the explicit table as the method table, then call this (before the
+ * first solve); ERKStep's defaults: safety 0.99, growth 25
+ * (arkode_erkstep_io.c:308-341). */
+void arkstep_port_set_erk(void* mem)
+{
+  ArkPort* m = (ArkPort*)mem;
+  m->erk     = 1;
+  m->safety  = 0.99;
+  m->growth  = 25.0;
 }
 
 /* ARKodeSetNonlinearSolver(SUNNonlinSol_FixedPoint(y, depth)) with no linear

@@ -215,14 +215,14 @@ def run_port_serial(q: Params, fixed_point=None, adams=False):
 
 
 def run_reference_arkode(q: Params, threads=None, imex=False, order=3, task_local=False,
-                         fixed_point=None):
+                         fixed_point=None, erk=False, mxstep=100000):
     """The benchmark's ARK-DIRK (arkode_driver.cpp:51-160) or, imex, ARK-IMEX
     (239-370; task_local: with --nls tl-newton) configuration through the
     reference's ARKodeEvolve: (counters, reals, solutions, Butcher tables)."""
     from . import arkstep as ak
     return ak.run_reference_with(lambda L: SerialBruss(L, q), initial(q), q.touts, q.rtol, q.atol,
                                  order=order, threads=threads, imex=imex, task_local=task_local,
-                                 fixed_point=fixed_point)
+                                 fixed_point=fixed_point, erk=erk, mxstep=mxstep)
 
 
 def run_port_serial_arkode(q: Params, tables, task_local=False, fixed_point=None):

@@ -16,6 +16,9 @@ difference-quotient J v and PSolve = the per-cell reaction solve; and
   solve as its linear solve and no SUNLinearSolver (the wrapper restated in
   oracle/arkstep.py around the reference's own SUNNonlinSol_Newton: the
   reference's build here has no MPI for the MPIPlusX vector it requires);
+* ``erk_``: the ERK configuration (ERKStep, 441-540, order 3), explicit on
+  the stiff reaction, so stability holds its steps near 1e-5: over
+  ``--tf 0.01 --nout 2`` (its own ``touts``);
 * ``fpdirk_`` / ``fpimex_``: ARK-DIRK / ARK-IMEX with ``--nls fixedpoint``
   (SUNNonlinSol_FixedPoint, Anderson depth 3, no linear solver), whose steps
   the stiff reaction limits to ~1e-5: over ``--tf 0.01 --nout 2`` (their own
@@ -32,6 +35,8 @@ summation order of its reductions).
 
 Usage (where the reference sources exist):
     python -m sundials_gb300.build && python tests/golden/gen_bruss3d_arkode_golden.py
+    (``--only erk_`` regenerates one configuration's entries and keeps the
+    file's others, their reduction-order samples included)
 """
 import sys
 from pathlib import Path
@@ -48,26 +53,35 @@ THREADS = (2, 3, 4, 6, 8, 16)
 NPTS = 16
 
 
-def main():
+CONFIGS = (("dirk_", False, False, None, False), ("imex_", True, False, None, False),
+           ("tl_", True, True, None, False), ("erk_", False, False, None, True),
+           ("fpdirk_", False, False, 3, False), ("fpimex_", True, False, 3, False))
+
+
+def main(only=None):
     q = bc.Params(NPTS, NPTS, NPTS)
     out = {"grid": np.array([NPTS] * 3), "touts": np.array(q.touts),
            "tol": np.array([q.rtol, q.atol]), "u0": bc.initial(q),
            "omp_threads": np.array(THREADS)}
-    qfp = bc.Params(NPTS, NPTS, NPTS, tf=0.01, nout=2)
-    for name, imex, tl, fp in (("dirk_", False, False, None), ("imex_", True, False, None),
-                               ("tl_", True, True, None), ("fpdirk_", False, False, 3),
-                               ("fpimex_", True, False, 3)):
-        qq = qfp if fp else q
-        if fp:
+    if only:
+        old = np.load(OUT)
+        out = {k: old[k] for k in old.files if not k.startswith(only)}
+    qshort = bc.Params(NPTS, NPTS, NPTS, tf=0.01, nout=2)
+    for name, imex, tl, fp, erk in CONFIGS:
+        if only and name != only:
+            continue
+        qq = qshort if (fp or erk) else q
+        if fp or erk:
             out[name + "touts"] = np.array(qq.touts)
-        c, r, s, tables = bc.run_reference_arkode(qq, imex=imex, task_local=tl, fixed_point=fp)
+        c, r, s, tables = bc.run_reference_arkode(qq, imex=imex, task_local=tl, fixed_point=fp,
+                                                  erk=erk)
         out.update({name + "counters": c, name + "reals": r, name + "y_last": s[-1],
                     **ak.tables_to_dict(tables, name)})
         print(name, dict(zip(ak.COUNTER_NAMES, c[-1].tolist())))
         oc, ow = [], []
         for th in THREADS:
             c2, _, s2, _ = bc.run_reference_arkode(qq, threads=th, imex=imex, task_local=tl,
-                                                   fixed_point=fp)
+                                                   fixed_point=fp, erk=erk)
             w = 1.0 / (q.rtol * np.abs(s) + q.atol)
             oc.append(c2[-1])
             ow.append(float(np.sqrt(np.mean(((s2 - s) * w) ** 2, axis=1)).max()))
@@ -81,4 +95,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[2] if len(sys.argv) > 2 and sys.argv[1] == "--only" else None)

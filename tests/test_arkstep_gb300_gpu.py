@@ -96,3 +96,33 @@ def test_arkstep_bruss3d_fixed_point_matches_reference(name, fma):
     yr = g[name + "y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
     assert w <= max(3.0 * float(g[name + "omp_wrms"].max()), 1e-6), w
+
+
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_erkstep_bruss3d_matches_reference(fma):
+    """The benchmark's ERK configuration (ERKStep, order 3, explicit on the
+    stiff reaction: ~800 steps over t in [0, 0.01]) on NVECTOR_GB300 with the
+    device right-hand side.  The reference's own reduction-order runs never
+    moved a counter, so every counter after every output must equal the
+    reference's; the last solution within 3x its own weighted RMS deviation
+    or 1e-3 tolerances (its own deviation, ~1e-5 tolerances, is below what
+    one rounding per product in the FMA mode moves over the run)."""
+    from sundials_gb300.bruss3d import Bruss3D
+    from sundials_gb300.nvector import NVector
+    g = np.load(GOLDEN)
+    rtol, atol = (float(v) for v in g["tol"])
+    tables = ak.tables_from(g, "erk_")
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    P = Bruss3D(*(int(v) for v in g["grid"]))
+    try:
+        _, f, _, _, data = P.arkode_callbacks()
+        c, r, s = ak.run_port(y.v, None, (None, f, None, None, data), lambda h: y.get(),
+                              [float(t) for t in g["erk_touts"]], tables, rtol, atol)
+    finally:
+        P.free()
+    ref = g["erk_counters"]
+    assert np.array_equal(c, ref), dict(zip(ak.COUNTER_NAMES, (c[-1] - ref[-1]).tolist()))
+    yr = g["erk_y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
+    assert w <= max(3.0 * float(g["erk_omp_wrms"].max()), 1e-3), w

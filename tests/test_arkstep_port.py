@@ -124,3 +124,44 @@ def test_fixed_point_golden_reproduced(name):
     assert np.array_equal(c, g[name + "counters"])
     assert np.array_equal(r.view(np.int64), g[name + "reals"].view(np.int64))
     assert np.array_equal(s[-1].view(np.int64), g[name + "y_last"].view(np.int64))
+
+
+def test_erk_golden_layout():
+    g = np.load(GOLDEN)
+    T = ak.tables_from(g, "erk_")
+    assert T["erk"] and T["e"] is None and tuple(T["i"]["orders"]) == (3, 2)
+    assert np.all(np.triu(T["i"]["A"]) == 0.0)  # explicit
+    last = dict(zip(ak.COUNTER_NAMES, g["erk_counters"][-1]))
+    assert last["nfe"] > 0 and last["nfi"] == last["nni"] == last["nli"] == 0
+    assert np.all(g["erk_omp_counters"] == g["erk_counters"][-1])
+
+
+@needs_ref
+@pytest.mark.parametrize("order,shape,c,tf,k", [(3, (6, 5, 7), 0.01, 0.01, None),
+                                                 (4, (6, 5, 7), -0.02, 0.01, None),
+                                                 (2, (5, 6, 4), 0.01, 0.005, None),
+                                                 (3, (6, 5, 7), 0.01, 10.0, (1, 1, 1, 1, 1, 1))])
+def test_erk_bit_identical_to_reference(order, shape, c, tf, k):
+    """The benchmark's ERK configuration (ERKStepCreate, arkode_driver.cpp:
+    441-540) through the restatement's ERKStep mode: stiff (steps held near
+    1e-5 by stability, many error-test failures at order 2) and non-stiff."""
+    q = bc.Params(*shape, c=c, tf=tf, nout=2, **({} if k is None else {"k": k}))
+    u0 = bc.initial(q)
+    c_ref, r_ref, s_ref, tables = ak.run_reference_with(lambda L: bc.SerialBruss(L, q), u0,
+                                                        q.touts, q.rtol, q.atol, order=order,
+                                                        erk=True)
+    c_p, r_p, s_p = ak.run_port_serial_with(lambda L: bc.SerialBruss(L, q), u0, q.touts, tables,
+                                            q.rtol, q.atol)
+    assert np.array_equal(c_p, c_ref), (c_p[-1] - c_ref[-1]).tolist()
+    assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
+    assert np.array_equal(s_p.view(np.int64), s_ref.view(np.int64))
+
+
+@needs_ref
+def test_erk_golden_reproduced():
+    g = np.load(GOLDEN)
+    q = bc.Params(*(int(v) for v in g["grid"]), tf=0.01, nout=2)
+    c, r, s = bc.run_port_serial_arkode(q, ak.tables_from(g, "erk_"))
+    assert np.array_equal(c, g["erk_counters"])
+    assert np.array_equal(r.view(np.int64), g["erk_reals"].view(np.int64))
+    assert np.array_equal(s[-1].view(np.int64), g["erk_y_last"].view(np.int64))
