@@ -10,7 +10,9 @@ import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
 INCLUDE = ROOT / "include"
-REF_INCLUDE = Path("/root/reference/include")
+from sundials_gb300 import build as _build  # noqa: E402
+
+REF_INCLUDE = _build.REFERENCE_SRC / "include"
 
 
 def declared_functions():
