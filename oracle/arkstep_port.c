@@ -50,7 +50,7 @@
  *   arkLsDQJtimes, arkLsPSolve, arkLsSolve
  *                                  src/arkode/arkode_ls.c:50-300, 2319-2456, 2842-2880,
  *                                  2981-3160, 3308-3520
- *   Hermite interpolation module (degree <= 3)   src/arkode/arkode_interp.c:97-170, 307-560
+ *   Hermite interpolation module (degree <= 4)   src/arkode/arkode_interp.c:97-170, 307-640
  *   N_VLinearCombination dispatch  src/sundials/sundials_nvector.c:549-580
  */
 #include <float.h>
@@ -130,7 +130,7 @@ typedef struct
   double Ae[MAXS][MAXS], be[MAXS], ce[MAXS], de[MAXS]; /* explicit table */
   /* vectors (ycur is the caller's output vector, as in ARKodeEvolve) */
   N_Vector yn, fn, ycur, ewt, tempv1, tempv2, tempv3, sdata, zpred, zcor, delta;
-  N_Vector Fi[MAXS], Fe[MAXS], ls_x, ls_ytemp, yold, fold;
+  N_Vector Fi[MAXS], Fe[MAXS], ls_x, ls_ytemp, yold, fold, fa;
   /* integrator state */
   double tn, tcur, h, hold, hprime, next_h, eta, h0u, tretlast, tolsf;
   double etamax;
@@ -784,24 +784,22 @@ static int complete_step(ArkPort* m, double dsm)
   return ARK_SUCCESS;
 }
 
-/* ARKodeGetDky(t, 0) with the Hermite interpolant of degree min(5, deg) */
-static int get_dky(ArkPort* m, double t, N_Vector dky)
+/* arkInterpEvaluate_Hermite, d = 0 (arkode_interp.c:441-700): the Hermite
+ * interpolant of degree min(order, deg) at tnew + tau (tnew - told); the
+ * quartic one bootstraps from the cubic at tau = -1/3 and the full
+ * right-hand side there (into fa) */
+static int interp_eval(ArkPort* m, double tau, int order, N_Vector dky)
 {
-  double tfuzz = FUZZ_FACTOR * UROUND * (fabs(m->tcur) + fabs(m->hold));
-  if (m->hold < 0.0) tfuzz = -tfuzz;
-  const double tp  = m->tcur - m->hold - tfuzz;
-  const double tn1 = m->tcur + tfuzz;
-  if ((t - tp) * (t - tn1) > 0.0) return ARK_BAD_T;
-  const double tau = (t - m->tcur) / m->h;
   if (!m->fn_is_current)
   {
     if (full_rhs(m, m->tn, m->yn, m->fn, FULLRHS_END)) return ARK_RHSFUNC_FAIL;
     m->fn_is_current = SUNTRUE;
   }
-  const int qd     = m->interp_degree < INTERP_MAX_DEGREE ? m->interp_degree : INTERP_MAX_DEGREE;
-  const double tau2 = tau * tau, tau3 = tau * tau2, h = m->hint_h;
-  double a[4];
-  N_Vector X[4];
+  int qd = order > 0 ? order : 0;
+  if (qd > m->interp_degree) qd = m->interp_degree;
+  const double tau2 = tau * tau, tau3 = tau * tau2, tau4 = tau * tau3, h = m->hint_h;
+  double a[5];
+  N_Vector X[5];
   switch (qd)
   {
   case 0: v_linearsum(0.5, m->yold, 0.5, m->yn, dky); break;
@@ -826,9 +824,35 @@ static int get_dky(ArkPort* m, double t, N_Vector dky)
     X[3] = m->fn;
     v_lincomb(4, a, X, dky);
     break;
-  default: return ARK_ILL_INPUT; /* degree > 3 (methods of order > 4) not restated */
+  case 4:
+    if (interp_eval(m, -1.0 / 3.0, 3, dky) != 0) return ARK_RHSFUNC_FAIL;
+    if (full_rhs(m, m->hint_tnew - h / 3.0, dky, m->fa, FULLRHS_OTHER)) return ARK_RHSFUNC_FAIL;
+    a[0] = -6.0 * tau2 - 16.0 * tau3 - 9.0 * tau4;
+    a[1] = 1.0 + 6.0 * tau2 + 16.0 * tau3 + 9.0 * tau4;
+    a[2] = h * 0.25 * (-5.0 * tau2 - 14.0 * tau3 - 9.0 * tau4);
+    a[3] = h * (tau + 2.0 * tau2 + tau3);
+    a[4] = h * 27.0 * 0.25 * (-tau4 - 2.0 * tau3 - tau2);
+    X[0] = m->yold;
+    X[1] = m->yn;
+    X[2] = m->fold;
+    X[3] = m->fn;
+    X[4] = m->fa;
+    v_lincomb(5, a, X, dky);
+    break;
+  default: return ARK_ILL_INPUT; /* quintic (degree 5) not restated */
   }
   return ARK_SUCCESS;
+}
+
+/* ARKodeGetDky(t, 0) */
+static int get_dky(ArkPort* m, double t, N_Vector dky)
+{
+  double tfuzz = FUZZ_FACTOR * UROUND * (fabs(m->tcur) + fabs(m->hold));
+  if (m->hold < 0.0) tfuzz = -tfuzz;
+  const double tp  = m->tcur - m->hold - tfuzz;
+  const double tn1 = m->tcur + tfuzz;
+  if ((t - tp) * (t - tn1) > 0.0) return ARK_BAD_T;
+  return interp_eval(m, (t - m->tcur) / m->h, INTERP_MAX_DEGREE, dky);
 }
 
 /* arkUpperBoundH0 */
@@ -978,6 +1002,7 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
   m->ls_ytemp = clone(y0);
   m->yold   = clone(y0);
   m->fold   = clone(y0);
+  m->fa     = clone(y0);
   for (int j = 0; j < stages; j++) m->Fi[j] = clone(y0);
   if (fe)
     for (int j = 0; j < stages; j++) m->Fe[j] = clone(y0);
@@ -1181,7 +1206,8 @@ void arkstep_port_free(void* mem)
   ArkPort* m = (ArkPort*)mem;
   if (!m) return;
   N_Vector vs[] = {m->yn,   m->fn,    m->ewt,  m->tempv1, m->tempv2,   m->tempv3, m->sdata,
-                   m->zpred, m->zcor, m->delta, m->ls_x,  m->ls_ytemp, m->yold,   m->fold};
+                   m->zpred, m->zcor, m->delta, m->ls_x,  m->ls_ytemp, m->yold,   m->fold,
+                   m->fa};
   for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); i++)
     if (vs[i]) vs[i]->ops->nvdestroy(vs[i]);
   for (int j = 0; j < m->s; j++)

@@ -1,7 +1,7 @@
 """CPU: the ARKStep restatement (oracle/arkstep_port.c) against the
 reference's own ARKodeEvolve, both on the reference's NVECTOR_SERIAL and
 SUNLINSOL_SPGMR, on the 3-D advection-reaction benchmark's ARK-DIRK and
-ARK-IMEX configurations (arkode_driver.cpp:51-160, 239-370) at orders 2-4 and
+ARK-IMEX configurations (arkode_driver.cpp:51-160, 239-370) at orders 2-5 and
 on ARK-IMEX with its task-local Newton (546-780, one task), and on both with
 ``--nls fixedpoint`` (SUNNonlinSol_FixedPoint, Anderson depth 3), with the
 benchmark's user functions restated in oracle/bruss3d_cvode.py:
@@ -56,7 +56,8 @@ def test_golden_layout(name):
 @pytest.mark.parametrize("imex,tl", [(False, False), (True, False), (True, True)],
                          ids=["dirk", "imex", "imex_tl_newton"])
 @pytest.mark.parametrize("shape,c,order", [((6, 5, 7), 0.01, 3), ((6, 5, 7), -0.02, 4),
-                                           ((5, 6, 4), 0.01, 2), ((8, 8, 8), 0.01, 3)])
+                                           ((5, 6, 4), 0.01, 2), ((8, 8, 8), 0.01, 3),
+                                           ((6, 5, 7), 0.01, 5)])
 def test_port_bit_identical_to_reference(shape, c, order, imex, tl):
     q = bc.Params(*shape, c=c)
     u0 = bc.initial(q)
@@ -140,6 +141,7 @@ def test_erk_golden_layout():
 @pytest.mark.parametrize("order,shape,c,tf,k", [(3, (6, 5, 7), 0.01, 0.01, None),
                                                  (4, (6, 5, 7), -0.02, 0.01, None),
                                                  (2, (5, 6, 4), 0.01, 0.005, None),
+                                                 (5, (6, 5, 7), 0.01, 0.01, None),
                                                  (3, (6, 5, 7), 0.01, 10.0, (1, 1, 1, 1, 1, 1))])
 def test_erk_bit_identical_to_reference(order, shape, c, tf, k):
     """The benchmark's ERK configuration (ERKStepCreate, arkode_driver.cpp:
