@@ -50,7 +50,7 @@
  *   arkLsDQJtimes, arkLsPSolve, arkLsSolve
  *                                  src/arkode/arkode_ls.c:50-300, 2319-2456, 2842-2880,
  *                                  2981-3160, 3308-3520
- *   Hermite interpolation module (degree <= 4)   src/arkode/arkode_interp.c:97-170, 307-640
+ *   Hermite interpolation module    src/arkode/arkode_interp.c:97-170, 307-790
  *   N_VLinearCombination dispatch  src/sundials/sundials_nvector.c:549-580
  */
 #include <float.h>
@@ -130,7 +130,7 @@ typedef struct
   double Ae[MAXS][MAXS], be[MAXS], ce[MAXS], de[MAXS]; /* explicit table */
   /* vectors (ycur is the caller's output vector, as in ARKodeEvolve) */
   N_Vector yn, fn, ycur, ewt, tempv1, tempv2, tempv3, sdata, zpred, zcor, delta;
-  N_Vector Fi[MAXS], Fe[MAXS], ls_x, ls_ytemp, yold, fold, fa;
+  N_Vector Fi[MAXS], Fe[MAXS], ls_x, ls_ytemp, yold, fold, fa, fb;
   /* integrator state */
   double tn, tcur, h, hold, hprime, next_h, eta, h0u, tretlast, tolsf;
   double etamax;
@@ -787,7 +787,8 @@ static int complete_step(ArkPort* m, double dsm)
 /* arkInterpEvaluate_Hermite, d = 0 (arkode_interp.c:441-700): the Hermite
  * interpolant of degree min(order, deg) at tnew + tau (tnew - told); the
  * quartic one bootstraps from the cubic at tau = -1/3 and the full
- * right-hand side there (into fa) */
+ * right-hand side there (into fa), the quintic one from quartics at -1/3
+ * and -2/3 (fa, fb) */
 static int interp_eval(ArkPort* m, double tau, int order, N_Vector dky)
 {
   if (!m->fn_is_current)
@@ -797,9 +798,10 @@ static int interp_eval(ArkPort* m, double tau, int order, N_Vector dky)
   }
   int qd = order > 0 ? order : 0;
   if (qd > m->interp_degree) qd = m->interp_degree;
-  const double tau2 = tau * tau, tau3 = tau * tau2, tau4 = tau * tau3, h = m->hint_h;
-  double a[5];
-  N_Vector X[5];
+  const double tau2 = tau * tau, tau3 = tau * tau2, tau4 = tau * tau3, tau5 = tau * tau4;
+  const double h = m->hint_h;
+  double a[6];
+  N_Vector X[6];
   switch (qd)
   {
   case 0: v_linearsum(0.5, m->yold, 0.5, m->yn, dky); break;
@@ -839,7 +841,27 @@ static int interp_eval(ArkPort* m, double tau, int order, N_Vector dky)
     X[4] = m->fa;
     v_lincomb(5, a, X, dky);
     break;
-  default: return ARK_ILL_INPUT; /* quintic (degree 5) not restated */
+  case 5: /* from quartics at tau = -1/3 and -2/3 and the right-hand side there */
+    if (interp_eval(m, -1.0 / 3.0, 4, dky) != 0) return ARK_RHSFUNC_FAIL;
+    if (full_rhs(m, m->hint_tnew - h / 3.0, dky, m->fa, FULLRHS_OTHER)) return ARK_RHSFUNC_FAIL;
+    if (interp_eval(m, -2.0 / 3.0, 4, dky) != 0) return ARK_RHSFUNC_FAIL;
+    if (full_rhs(m, m->hint_tnew - h * 2.0 / 3.0, dky, m->fb, FULLRHS_OTHER))
+      return ARK_RHSFUNC_FAIL;
+    a[0] = 54.0 * tau5 + 135.0 * tau4 + 110.0 * tau3 + 30.0 * tau2;
+    a[1] = 1.0 - a[0];
+    a[2] = h / 4.0 * (27.0 * tau5 + 63.0 * tau4 + 49.0 * tau3 + 13.0 * tau2);
+    a[3] = h / 4.0 * (27.0 * tau5 + 72.0 * tau4 + 67.0 * tau3 + 26.0 * tau2 + 4.0 * tau);
+    a[4] = h / 4.0 * (81.0 * tau5 + 189.0 * tau4 + 135.0 * tau3 + 27.0 * tau2);
+    a[5] = h / 4.0 * (81.0 * tau5 + 216.0 * tau4 + 189.0 * tau3 + 54.0 * tau2);
+    X[0] = m->yold;
+    X[1] = m->yn;
+    X[2] = m->fold;
+    X[3] = m->fn;
+    X[4] = m->fa;
+    X[5] = m->fb;
+    v_lincomb(6, a, X, dky);
+    break;
+  default: return ARK_ILL_INPUT;
   }
   return ARK_SUCCESS;
 }
@@ -1003,6 +1025,7 @@ void* arkstep_port_create(ArkRhsFn fe, ArkRhsFn fi, double t0, N_Vector y0, doub
   m->yold   = clone(y0);
   m->fold   = clone(y0);
   m->fa     = clone(y0);
+  m->fb     = clone(y0);
   for (int j = 0; j < stages; j++) m->Fi[j] = clone(y0);
   if (fe)
     for (int j = 0; j < stages; j++) m->Fe[j] = clone(y0);
@@ -1207,7 +1230,7 @@ void arkstep_port_free(void* mem)
   if (!m) return;
   N_Vector vs[] = {m->yn,   m->fn,    m->ewt,  m->tempv1, m->tempv2,   m->tempv3, m->sdata,
                    m->zpred, m->zcor, m->delta, m->ls_x,  m->ls_ytemp, m->yold,   m->fold,
-                   m->fa};
+                   m->fa,    m->fb};
   for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); i++)
     if (vs[i]) vs[i]->ops->nvdestroy(vs[i]);
   for (int j = 0; j < m->s; j++)

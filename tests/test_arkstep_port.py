@@ -142,11 +142,14 @@ def test_erk_golden_layout():
                                                  (4, (6, 5, 7), -0.02, 0.01, None),
                                                  (2, (5, 6, 4), 0.01, 0.005, None),
                                                  (5, (6, 5, 7), 0.01, 0.01, None),
+                                                 (6, (6, 5, 7), 0.01, 0.01, None),
+                                                 (9, (6, 5, 7), -0.02, 0.01, None),
                                                  (3, (6, 5, 7), 0.01, 10.0, (1, 1, 1, 1, 1, 1))])
 def test_erk_bit_identical_to_reference(order, shape, c, tf, k):
     """The benchmark's ERK configuration (ERKStepCreate, arkode_driver.cpp:
     441-540) through the restatement's ERKStep mode: stiff (steps held near
-    1e-5 by stability, many error-test failures at order 2) and non-stiff."""
+    1e-5 by stability, many error-test failures at order 2) and non-stiff;
+    orders 6 and 9 take the quintic dense output."""
     q = bc.Params(*shape, c=c, tf=tf, nout=2, **({} if k is None else {"k": k}))
     u0 = bc.initial(q)
     c_ref, r_ref, s_ref, tables = ak.run_reference_with(lambda L: bc.SerialBruss(L, q), u0,
