@@ -24,7 +24,7 @@ from . import heat_cvode as hc
 from . import port
 
 COUNTER_NAMES = ("nst", "nst_attempts", "nfi", "netf", "ncfn", "nni", "nnf", "nli", "nps",
-                 "njtimes", "nfeDQ", "ncfl", "nfe", "nnlfi")
+                 "njtimes", "nfeDQ", "ncfl", "nfe", "nnlfi", "nsetups", "nje")
 REAL_NAMES = ("hold", "hnext", "tcur", "h0u")
 TABLE_KEYS = ("A", "b", "c", "d", "orders")
 
@@ -65,6 +65,8 @@ def ref_lib() -> ct.CDLL:
         ("ARKStepCreate", VP, [VP, VP, D, VP, VP]),
         ("ARKodeSetOrder", I, [VP, I]),
         ("ARKodeSStolerances", I, [VP, D, D]),
+        ("ARKodeSVtolerances", I, [VP, D, VP]),
+        ("ARKodeSetJacFn", I, [VP, VP]),
         ("ARKodeSetMaxNumSteps", I, [VP, ct.c_long]),
         ("SUNNonlinSol_Newton", VP, [VP, VP]),
         ("SUNNonlinSolFree", I, [VP]),
@@ -98,7 +100,7 @@ def ref_lib() -> ct.CDLL:
                  "ARKodeGetNumStepSolveFails", "ARKodeGetNumNonlinSolvIters",
                  "ARKodeGetNumNonlinSolvConvFails", "ARKodeGetNumLinIters",
                  "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals", "ARKodeGetNumLinRhsEvals",
-                 "ARKodeGetNumLinConvFails"):
+                 "ARKodeGetNumLinConvFails", "ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals"):
         f = getattr(L, name)
         f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
     for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
@@ -128,6 +130,10 @@ def port_lib() -> ct.CDLL:
         L.arkstep_port_set_fixed_point.argtypes = [VP, I]
         L.arkstep_port_set_erk.restype = None
         L.arkstep_port_set_erk.argtypes = [VP]
+        L.arkstep_port_set_matrix.restype = None
+        L.arkstep_port_set_matrix.argtypes = [VP, VP, VP]
+        L.arkstep_port_set_vabstol.restype = None
+        L.arkstep_port_set_vabstol.argtypes = [VP, D, VP]
         L._arkstep_declared = True
     return L
 
@@ -236,7 +242,7 @@ def _read_table(T: _Table) -> dict:
 
 
 def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=100000, threads=None,
-                       imex=False, task_local=False, fixed_point=None, erk=False):
+                       imex=False, task_local=False, fixed_point=None, erk=False, direct=False):
     """The reference's ARKodeEvolve on the problem whose serial callbacks
     make_serial(L) builds (.addresses() -> (f, jtimes, psetup, psolve), with
     psetup None, .imex_addresses() -> (fe, fi), and .arr(N_Vector)):
@@ -247,7 +253,10 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     problem's .reaction_into / .block_solve; the counters then end with its
     nonlinear-residual evaluations.  fixed_point = m: SUNNonlinSol_FixedPoint
     with Anderson depth m and no linear solver (``--nls fixedpoint``).
-    erk: the benchmark's ERK configuration (ERKStepCreate(f), no nonlinear
+    direct: SUNDenseMatrix + SUNLINSOL_DENSE and the problem's
+    .jac_address() (ARKodeSetJacFn) instead of SPGMR: the matrix-based path
+    of ARKLS.  atol: a scalar (ARKodeSStolerances) or an array
+    (ARKodeSVtolerances).  erk: the benchmark's ERK configuration (ERKStepCreate(f), no nonlinear
     or linear solver; the method's table is returned as tables["i"] with
     tables["erk"] set).  threads = k: NVECTOR_OPENMP on k threads
     instead of NVECTOR_SERIAL (its reductions sum in another order)."""
@@ -259,17 +268,30 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     y = L.N_VNew_Serial(n, ctx) if threads is None else L.N_VNew_OpenMP(n, threads, ctx)
     prob.arr(y)[:] = u0
     f, jt, ps, pv = prob.addresses()
-    assert ps is None and jt is None
+    assert direct or (ps is None and jt is None)
     fe, fi = prob.imex_addresses() if imex else (None, f)
     mem = L.ERKStepCreate(f, 0.0, y, ctx) if erk else L.ARKStepCreate(fe, fi, 0.0, y, ctx)
     assert mem
     assert L.ARKodeSetOrder(mem, order) == 0
-    assert L.ARKodeSStolerances(mem, rtol, atol) == 0
+    vatol = None
+    if np.ndim(atol) == 0:
+        assert L.ARKodeSStolerances(mem, rtol, atol) == 0
+    else:
+        vatol = L.N_VNew_Serial(n, ctx)
+        prob.arr(vatol)[:] = atol
+        assert L.ARKodeSVtolerances(mem, rtol, vatol) == 0
     assert L.ARKodeSetMaxNumSteps(mem, mxstep) == 0
-    TL, LS, NLS = None, None, None
+    TL, LS, NLS, A = None, None, None, None
     no_ls = task_local or fixed_point is not None or erk
     if erk:
         pass
+    elif direct:
+        NLS = L.SUNNonlinSol_Newton(y, ctx)
+        assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
+        A = L.SUNDenseMatrix(n, n, ctx)
+        LS = L.SUNLinSol_Dense(y, A, ctx)
+        assert L.ARKodeSetLinearSolver(mem, LS, A) == 0
+        assert L.ARKodeSetJacFn(mem, prob.jac_address()) == 0
     elif fixed_point is not None:
         NLS = L.SUNNonlinSol_FixedPoint(y, fixed_point, ctx)
         assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
@@ -313,7 +335,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
                      "ARKodeGetNumNonlinSolvIters", "ARKodeGetNumNonlinSolvConvFails",
                      "ARKodeGetNumLinIters", "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals",
                      "ARKodeGetNumLinRhsEvals", "ARKodeGetNumLinConvFails"):
-            if (no_ls and any(k in name for k in ("Lin", "Prec", "Jtimes"))
+            if (no_ls and any(k in name for k in ("Lin", "Prec", "Jtimes", "Jac"))
                     or erk and "Nonlin" in name):
                 row.append(0)  # no linear solver attached
                 continue
@@ -322,6 +344,12 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         L.ARKodeGetNumRhsEvals(mem, 0, ct.byref(c))
         row.append(c.value)
         row.append(TL.nnlfi if TL else 0)
+        for name in ("ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals"):
+            if LS:
+                getattr(L, name)(mem, ct.byref(c))
+                row.append(c.value)
+            else:
+                row.append(0)
         rrow = []
         for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
                      "ARKodeGetActualInitStep"):
@@ -338,13 +366,17 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         L.SUNNonlinSolFree(NLS)
     if LS:
         L.SUNLinSolFree(LS)
+    if A:
+        L.SUNMatDestroy(A)
+    if vatol:
+        L.N_VDestroy(vatol)
     L.N_VDestroy(y)
     L.SUNContext_Free(ct.byref(ctx))
     return np.array(cnt, np.int64), np.array(real), np.array(sols), table
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000,
-             block_solve=None, fixed_point=None):
+             block_solve=None, fixed_point=None, matrix=None, vatol_handle=None):
     """The restated ARKStep on the objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (fe, fi, jtimes, psolve,
@@ -353,7 +385,9 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     run_reference_with ({"i": ..., "e": ... or None}); block_solve: the
     address of a block solve (z, x, b, gamma, user_data) -> the task-local
     Newton, with LS_handle and the preconditioner None; fixed_point = m: the
-    fixed-point solver with Anderson depth m, also without a linear solver."""
+    fixed-point solver with Anderson depth m, also without a linear solver;
+    matrix = (SUNMatrix, ARKLsJacFn address): the matrix-based path with a
+    direct LS_handle; vatol_handle: an N_Vector of absolute tolerances."""
     P = port_lib()
     fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
@@ -371,7 +405,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
         return [x.ctypes.data_as(DP) for x in a]
 
     q, p = (int(v) for v in Ti["orders"])
-    mem = P.arkstep_port_create(fe, fi, 0.0, y0_handle, rtol, atol, mxstep, LS_handle, jt, pv,
+    mem = P.arkstep_port_create(fe, fi, 0.0, y0_handle, rtol, 0.0 if vatol_handle else atol,
+                                mxstep, LS_handle, jt, pv,
                                 data, len(Ti["b"]), q, p, *arrs(Ti), *arrs(Te))
     assert mem
     if block_solve is not None:
@@ -380,6 +415,10 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
         P.arkstep_port_set_fixed_point(mem, fixed_point)
     if tables.get("erk"):
         P.arkstep_port_set_erk(mem)
+    if matrix is not None:
+        P.arkstep_port_set_matrix(mem, matrix[0], matrix[1])
+    if vatol_handle:
+        P.arkstep_port_set_vabstol(mem, rtol, vatol_handle)
     cnt, real, sols = [], [], []
     t = D()
     cbuf = (ct.c_long * len(COUNTER_NAMES))()
@@ -398,7 +437,7 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
 
 
 def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=False,
-                         fixed_point=None):
+                         fixed_point=None, direct=False):
     """run_port on the reference's own serial vector and SPGMR (the pin)."""
     L = ref_lib()
     ctx = VP()
@@ -407,16 +446,30 @@ def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=
     y = L.N_VNew_Serial(len(u0), ctx)
     prob.arr(y)[:] = u0
     no_ls = task_local or fixed_point is not None or tables.get("erk")
-    LS = None if no_ls else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    A, matrix, vatol = None, None, None
+    if direct:
+        A = L.SUNDenseMatrix(len(u0), len(u0), ctx)
+        LS = L.SUNLinSol_Dense(y, A, ctx)
+        matrix = (A, prob.jac_address())
+    else:
+        LS = None if no_ls else L.SUNLinSol_SPGMR(y, 1, 0, ctx)
+    if np.ndim(atol) != 0:
+        vatol = L.N_VNew_Serial(len(u0), ctx)
+        prob.arr(vatol)[:] = atol
     f, jt, _, pv = prob.addresses()
     fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)
     try:
-        return run_port(y, LS, (fe, fi, jt, None if no_ls else pv, None),
+        return run_port(y, LS, (fe, fi, None if direct else jt,
+                                None if (no_ls or direct) else pv, None),
                         lambda h: prob.arr(h).copy(), touts, tables, rtol, atol,
                         block_solve=prob.block_solve_address() if task_local else None,
-                        fixed_point=fixed_point)
+                        fixed_point=fixed_point, matrix=matrix, vatol_handle=vatol)
     finally:
         if LS:
             L.SUNLinSolFree(LS)
+        if A:
+            L.SUNMatDestroy(A)
+        if vatol:
+            L.N_VDestroy(vatol)
         L.N_VDestroy(y)
         L.SUNContext_Free(ct.byref(ctx))

@@ -47,7 +47,8 @@
  *                                  src/arkode/arkode_arkstep_nls.c:364-604, 1152-1200
  *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-310
  *   ARKodeSetLinearSolver defaults, arkLsInitialize, arkLsATimes,
- *   arkLsDQJtimes, arkLsPSolve, arkLsSolve
+ *   arkLsDQJtimes, arkLsPSolve, arkLsLinSys, arkLsSetup, arkLsSolve
+ *   arkStep_NlsLSetup              arkode_arkstep_nls.c:472-512
  *                                  src/arkode/arkode_ls.c:50-300, 2319-2456, 2842-2880,
  *                                  2981-3160, 3308-3520
  *   Hermite interpolation module    src/arkode/arkode_interp.c:97-170, 307-790
@@ -91,14 +92,18 @@
 #define RDIV 2.3
 #define NLSCOEF 0.1
 #define ARKLS_EPLIN 0.05
+#define ARKLS_MSBJ 51
+#define DGMAX 0.2
+#define MSBP 20
 #define INTERP_MAX_DEGREE 5
 
 enum { PREDICT_AGAIN = 3, CONV_FAIL = 4, TRY_AGAIN = 5, FIRST_CALL = 6, PREV_CONV_FAIL = 7,
        PREV_ERR_FAIL = 8, RHSFUNC_RECVR = 9 };
 enum { NLS_CONTINUE = 901, NLS_CONV_RECVR = 902 };
+enum { NO_FAILURES = 0, FAIL_BAD_J = 1, FAIL_OTHER = 2 };
 enum { FULLRHS_START = 0, FULLRHS_END = 1, FULLRHS_OTHER = 2 };
 enum { ARK_SUCCESS = 0, ARK_TOO_MUCH_WORK = -1, ARK_TOO_MUCH_ACC = -2, ARK_ERR_FAILURE = -3,
-       ARK_CONV_FAILURE = -4, ARK_LSOLVE_FAIL = -7, ARK_RHSFUNC_FAIL = -8,
+       ARK_CONV_FAILURE = -4, ARK_LSETUP_FAIL = -6, ARK_LSOLVE_FAIL = -7, ARK_RHSFUNC_FAIL = -8,
        ARK_REPTD_RHSFUNC_ERR = -10, ARK_UNREC_RHSFUNC_ERR = -11, ARK_TOO_CLOSE = -27,
        ARK_BAD_T = -25, ARK_ILL_INPUT = -22 };
 
@@ -108,6 +113,9 @@ typedef int (*ArkJTimesFn)(N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vect
                            void* user_data, N_Vector tmp);
 typedef int (*ArkPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
                            double gamma, double delta, int lr, void* user_data);
+/* ARKLsJacFn */
+typedef int (*ArkJacFn)(double t, N_Vector y, N_Vector fy, SUNMatrix J, void* user_data,
+                        N_Vector tmp1, N_Vector tmp2, N_Vector tmp3);
 /* the benchmark's block solve x = (I - gamma dfi/dy)^{-1} b at the state z
  * (rhs3D.hpp SolveReactionLinSys, called with x == b) */
 typedef int (*ArkBlockSolveFn)(N_Vector z, N_Vector x, N_Vector b, double gamma,
@@ -121,6 +129,11 @@ typedef struct
   ArkPSolveFn psolve;
   ArkBlockSolveFn block_lsolve; /* set: the task-local Newton, no SUNLinearSolver */
   FPPort* fp;                   /* set: the fixed-point solver, no SUNLinearSolver */
+  SUNMatrix Amat, savedJ;       /* set: a matrix-based (direct) linear solver */
+  ArkJacFn jac;
+  N_Vector Vabstol;             /* ARKodeSVtolerances' copy, or NULL */
+  int jcur, nls_jcur, jbad, convfail;
+  long nsetups, nje, nstlp, nstlj;
   void* user_data;
   double rtol, atol;
   long mxstep;
@@ -180,11 +193,15 @@ static double dmin(double a, double b) { return a < b ? a : b; }
 
 /* arkEwtSetSS (atol > 0, so no N_VMin test) */
 static void set_ewt(ArkPort* m, N_Vector ycur, N_Vector w)
-{
+{ /* arkEwtSetSS / arkEwtSetSV (all absolute tolerances > 0) */
   N_Vector t = m->tempv1;
   t->ops->nvabs(ycur, t);
-  v_scale(m->rtol, t, t);
-  t->ops->nvaddconst(t, m->atol, t);
+  if (m->Vabstol) v_linearsum(m->rtol, t, 1.0, m->Vabstol, t);
+  else
+  {
+    v_scale(m->rtol, t, t);
+    t->ops->nvaddconst(t, m->atol, t);
+  }
   t->ops->nvinv(t, w);
 }
 
@@ -335,9 +352,79 @@ static int ls_psolve(void* mem, N_Vector r, N_Vector z, double tol, int lr)
 }
 
 /* arkLsSolve, iterative and matrix-free (rwt = ewt) */
+/* arkLsLinSys (arkode_ls.c:2890-2975): A = I - gamma J, J new or saved */
+static int ls_linsys(ArkPort* m, double t, N_Vector y, N_Vector fy, int jok)
+{
+  if (jok)
+  {
+    m->jcur = SUNFALSE;
+    if (m->savedJ->ops->copy(m->savedJ, m->Amat)) return -1;
+  }
+  else
+  {
+    m->jcur = SUNTRUE;
+    if (m->Amat->ops->zero(m->Amat)) return -1;
+    int retval = m->jac(t, y, fy, m->Amat, m->user_data, m->tempv1, m->tempv2, m->tempv3);
+    if (retval < 0) return -1;
+    if (retval > 0) return 1;
+    if (m->Amat->ops->copy(m->Amat, m->savedJ)) return -1;
+  }
+  if (m->Amat->ops->scaleaddi(-m->gamma, m->Amat)) return -1;
+  return 0;
+}
+
+/* arkLsSetup with a matrix (arkode_ls.c:3166-3306) */
+static int ls_setup(ArkPort* m, int convfail, double tpred, N_Vector ypred, N_Vector fpred)
+{
+  m->ls_tcur             = tpred;
+  m->ls_ycur             = ypred;
+  m->ls_fcur             = fpred;
+  const int dgamma_fail  = fabs(m->gamrat - 1.0) >= DGMAX;
+  m->jbad = m->initsetup || (m->nst >= m->nstlj + ARKLS_MSBJ) ||
+            ((convfail == FAIL_BAD_J) && !dgamma_fail) || (convfail == FAIL_OTHER);
+  int retval = ls_linsys(m, tpred, ypred, fpred, !m->jbad);
+  if (m->jcur)
+  {
+    m->nje++;
+    m->nstlj = m->nst;
+  }
+  if (retval != 0) return retval;
+  return m->LS->ops->setup(m->LS, m->Amat);
+}
+
+/* arkLsSolve with a direct solver: no tolerance, x = A^{-1} b, the
+ * correction scaled by 2 / (1 + gamrat) when gamma changed since setup */
+static int ls_solve_direct(ArkPort* m, N_Vector b, double tnow, N_Vector ynow, N_Vector fnow,
+                           int mnewt)
+{
+  m->ls_tcur = tnow;
+  m->ls_ycur = ynow;
+  m->ls_fcur = fnow;
+  if (m->LS->ops->setscalingvectors) m->LS->ops->setscalingvectors(m->LS, m->ewt, m->ewt);
+  v_const(0.0, m->ls_x);
+  if (m->LS->ops->setzeroguess) m->LS->ops->setzeroguess(m->LS, SUNTRUE);
+  int retval = m->LS->ops->solve(m->LS, m->Amat, m->ls_x, b, 0.0);
+  v_scale(1.0, m->ls_x, b);
+  if (m->gamrat != 1.0) v_scale(2.0 / (1.0 + m->gamrat), b, b);
+  if (retval != 0) m->ncfl++;
+  switch (retval)
+  {
+  case 0: return 0;
+  case SUNLS_RES_REDUCED: return mnewt == 0 ? 0 : 1;
+  case SUNLS_CONV_FAIL:
+  case SUNLS_ATIMES_FAIL_REC:
+  case SUNLS_PSOLVE_FAIL_REC:
+  case SUNLS_PACKAGE_FAIL_REC:
+  case SUNLS_QRFACT_FAIL:
+  case SUNLS_LUFACT_FAIL: return 1;
+  default: return retval < 0 ? -1 : 0;
+  }
+}
+
 static int ls_solve(ArkPort* m, N_Vector b, double tnow, N_Vector ynow, N_Vector fnow,
                     double eRNrm, int mnewt)
 {
+  if (m->Amat) return ls_solve_direct(m, b, tnow, ynow, fnow, mnewt);
   m->ls_tcur        = tnow;
   m->ls_ycur        = ynow;
   m->ls_fcur        = fnow;
@@ -430,16 +517,41 @@ static int nls_convtest(ArkPort* m, N_Vector del, double tol, int mcur)
 /* SUNNonlinSolSolve_Newton without a linear solver setup function (the
  * matrix-free solver with no preconditioner setup disables it), so a
  * recoverable failure is never retried with a fresh setup. */
-static int newton_solve(ArkPort* m, N_Vector zcor, double tol)
+/* arkStep_NlsLSetup (arkode_arkstep_nls.c:472-512) */
+static int nls_lsetup(ArkPort* m, int jbad)
+{
+  if (jbad) m->convfail = FAIL_BAD_J;
+  m->nsetups++;
+  int retval    = ls_setup(m, m->convfail, m->tcur, m->ycur, m->Fi[m->istage]);
+  m->nls_jcur   = m->jcur;
+  m->firststage = SUNFALSE;
+  m->gamrat = m->crate = 1.0;
+  m->gammap            = m->gamma;
+  m->nstlp             = m->nst;
+  if (retval < 0) return ARK_LSETUP_FAIL;
+  if (retval > 0) return CONV_FAIL;
+  return 0;
+}
+
+/* SUNNonlinSolSolve_Newton; a recoverable failure is retried once with a
+ * fresh setup (jbad) when there is a linear solver setup (a matrix) and the
+ * Jacobian was not current */
+static int newton_solve(ArkPort* m, N_Vector zcor, double tol, int callLSetup)
 {
   N_Vector delta = m->delta;
-  int retval;
+  int retval, jbad = 0;
   m->niters     = 0;
   m->nconvfails = 0;
-  m->curiter    = 0;
-  retval        = nls_residual(m, zcor, delta);
-  if (retval == 0)
+  for (;;)
   {
+    m->curiter = 0;
+    retval     = nls_residual(m, zcor, delta);
+    if (retval != 0) break;
+    if (callLSetup)
+    {
+      retval = nls_lsetup(m, jbad);
+      if (retval != 0) break;
+    }
     for (;;)
     {
       m->niters++;
@@ -449,7 +561,11 @@ static int newton_solve(ArkPort* m, N_Vector zcor, double tol)
       v_linearsum(1.0, zcor, 1.0, delta, zcor);
       retval = nls_convtest(m, delta, tol, m->curiter);
       m->curiter++;
-      if (retval == 0) return 0;
+      if (retval == 0)
+      {
+        m->nls_jcur = SUNFALSE;
+        return 0;
+      }
       if (retval != NLS_CONTINUE) break;
       if (m->curiter >= MAXCOR)
       {
@@ -459,6 +575,15 @@ static int newton_solve(ArkPort* m, N_Vector zcor, double tol)
       retval = nls_residual(m, zcor, delta);
       if (retval != 0) break;
     }
+    if ((retval > 0) && !m->nls_jcur && m->Amat)
+    {
+      m->nconvfails++;
+      callLSetup = 1;
+      jbad       = 1;
+      v_const(0.0, zcor);
+      continue;
+    }
+    break;
   }
   m->nconvfails++;
   return retval;
@@ -484,13 +609,21 @@ static int fp_ctest(void* mem, N_Vector zcor, N_Vector del, double tol, int curi
   return nls_convtest((ArkPort*)mem, del, tol, curiter);
 }
 
-static int nls(ArkPort* m)
-{ /* arkStep_Nls with no lsetup */
-  m->crate = 1.0;
+static int nls(ArkPort* m, int nflag)
+{ /* arkStep_Nls: an lsetup exists only with a matrix-based linear solver */
+  int callLSetup = 0;
+  if (m->Amat)
+  {
+    m->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
+    callLSetup = m->firststage || (fabs(m->gamrat - 1.0) > DGMAX) ||
+                 (nflag == PREV_CONV_FAIL) || (nflag == PREV_ERR_FAIL) ||
+                 (m->nst >= m->nstlp + MSBP);
+  }
+  else m->crate = 1.0;
   v_const(0.0, m->zcor);
   m->eRNrm   = 0.1 * NLSCOEF;
   int retval = m->fp ? fp_port_solve(m->fp, m->zcor, NLSCOEF, fp_sys, fp_ctest, m)
-                     : newton_solve(m, m->zcor, NLSCOEF);
+                     : newton_solve(m, m->zcor, NLSCOEF, callLSetup);
   if (m->fp)
   {
     m->nls_iters += fp_port_niters(m->fp);
@@ -510,6 +643,7 @@ static int nls(ArkPort* m)
   }
   if (retval == 0)
   {
+    m->jcur = SUNFALSE;
     v_linearsum(1.0, m->zcor, 1.0, m->zpred, m->ycur);
     return ARK_SUCCESS;
   }
@@ -673,7 +807,7 @@ static int take_step(ArkPort* m, double* dsm, int* nflag)
     stage_setup(m, implicit_stage);
     if (implicit_stage)
     {
-      *nflag = nls(m);
+      *nflag = nls(m, *nflag);
       if (*nflag != ARK_SUCCESS) return TRY_AGAIN;
     }
     else v_linearsum(1.0, m->yn, 1.0, m->sdata, m->ycur);
@@ -1087,6 +1221,27 @@ void arkstep_port_set_task_local(void* mem, ArkBlockSolveFn block_lsolve)
   ((ArkPort*)mem)->block_lsolve = block_lsolve;
 }
 
+/* ARKodeSetLinearSolver(LS, A) with a matrix and a direct LS, and
+ * ARKodeSetJacFn(jac): the matrix-based path of ARKLS (create the object
+ * with LS and no psolve, then attach A and jac; the saved Jacobian is cloned
+ * from A as arkLsInitialize does). */
+void arkstep_port_set_matrix(void* mem, SUNMatrix A, ArkJacFn jac)
+{
+  ArkPort* m = (ArkPort*)mem;
+  m->Amat       = A;
+  m->jac     = jac;
+  if (!m->savedJ) m->savedJ = A->ops->clone(A);
+}
+
+/* ARKodeSVtolerances(rtol, abstol): a copy of abstol (all entries > 0). */
+void arkstep_port_set_vabstol(void* mem, double rtol, N_Vector abstol)
+{
+  ArkPort* m = (ArkPort*)mem;
+  m->rtol    = rtol;
+  if (!m->Vabstol) m->Vabstol = abstol->ops->nvclone(abstol);
+  v_scale(1.0, abstol, m->Vabstol);
+}
+
 /* ERKStepCreate(f, ...) instead of ARKStepCreate: create with fe NULL, fi = f
  * and the explicit table as the method table, then call this (before the
  * first solve); ERKStep's defaults: safety 0.99, growth 25
@@ -1200,7 +1355,7 @@ int arkstep_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 }
 
 /* counters: nst, nst_attempts, nfi, netf, ncfn, nni, nnf, nli, nps, njtimes,
- * nfeDQ, ncfl, nfe, nnlfi; reals: last step, next step, current time, first step */
+ * nfeDQ, ncfl, nfe, nnlfi, nsetups, nje; reals: last step, next step, current time, first step */
 void arkstep_port_stats(void* mem, long* cnt, double* r)
 {
   ArkPort* m = (ArkPort*)mem;
@@ -1218,6 +1373,8 @@ void arkstep_port_stats(void* mem, long* cnt, double* r)
   cnt[11]    = m->ncfl;
   cnt[12]    = m->nfe;
   cnt[13]    = m->nnlfi;
+  cnt[14]    = m->nsetups;
+  cnt[15]    = m->nje;
   r[0]       = m->hold;
   r[1]       = m->next_h;
   r[2]       = m->tcur;
@@ -1239,5 +1396,7 @@ void arkstep_port_free(void* mem)
     if (m->Fe[j]) m->Fe[j]->ops->nvdestroy(m->Fe[j]);
   }
   fp_port_free(m->fp);
+  if (m->savedJ) m->savedJ->ops->destroy(m->savedJ);
+  if (m->Vabstol) m->Vabstol->ops->nvdestroy(m->Vabstol);
   free(m);
 }

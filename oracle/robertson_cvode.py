@@ -219,3 +219,25 @@ def run_reference_direct(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, threads
     atol = vector_atol(ncells) if atol is None else atol
     return hc.run_reference_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
                                  atol, threads=threads, direct=True)
+
+
+def run_reference_arkode_direct(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, threads=None):
+    """The same problem through the reference's ARKStep (DIRK, order 3,
+    Newton) with the matrix-based direct path of ARKLS: SUNDenseMatrix +
+    SUNLINSOL_DENSE and the user Jacobian (ARKodeSetJacFn), per-species
+    absolute tolerances (ARKodeSVtolerances): (counters, reals, solutions,
+    Butcher tables)."""
+    from . import arkstep as ak
+    k = rates(ncells)
+    atol = vector_atol(ncells) if atol is None else atol
+    return ak.run_reference_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
+                                 atol, threads=threads, direct=True)
+
+
+def run_port_serial_arkode_direct(ncells: int, tables, touts=TOUTS, rtol=1e-4, atol=None):
+    """The same through the ARKStep restatement on the reference's objects."""
+    from . import arkstep as ak
+    k = rates(ncells)
+    atol = vector_atol(ncells) if atol is None else atol
+    return ak.run_port_serial_with(lambda L: SerialRobertson(L, k), initial(ncells), touts,
+                                   tables, rtol, atol, direct=True)

@@ -126,3 +126,43 @@ def test_erkstep_bruss3d_matches_reference(fma):
     yr = g["erk_y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + atol)) ** 2)))
     assert w <= max(3.0 * float(g["erk_omp_wrms"].max()), 1e-3), w
+
+
+ROB_GOLDEN = Path(__file__).resolve().parent / "golden" / "robertson_arkode_ref.npz"
+
+
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_arkstep_robertson_direct_block_lu_matches_reference(fma):
+    """The batched Robertson cells (64) through ARKStep with
+    SUNMatrix_BlockDiag_GB300 + SUNLinSol_BlockLU_GB300 (FP64) attached as
+    ARKODE's direct linear solver (ARKodeSetLinearSolver(LS, A)) and the
+    device Jacobian (ARKodeSetJacFn), per-species absolute tolerances, to
+    t = 4e5: against the reference's ARKodeEvolve with SUNDenseMatrix +
+    SUNLINSOL_DENSE.  Its own reduction-order runs never moved a counter, so
+    every counter after every output must equal the reference's; the last
+    solution within 3x its own weighted RMS deviation and 10 tolerances."""
+    from sundials_gb300 import blockdiag as BD
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.robertson import LU_FP64, Robertson
+    g = np.load(ROB_GOLDEN)
+    ncells = int(g["cells"])
+    rtol = float(g["rtol"])
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    vatol = NVector.from_numpy(g["atol"])
+    prob = Robertson(g["k"], y, LU_FP64)
+    M = BD.BlockDiag([3] * ncells)
+    S = BD.BlockLU(y.v, M, LU_FP64)
+    try:
+        f = prob.cvode_callbacks()[0]
+        c, r, s = ak.run_port(y.v, S.S, (None, f, None, None, prob.p), lambda h: y.get(),
+                              [float(t) for t in g["touts"]], ak.tables_from(g), rtol, 0.0,
+                              matrix=(M.A, prob.jac_address()), vatol_handle=vatol.v)
+    finally:
+        S.free()
+        prob.free()
+    ref = g["counters"]
+    assert np.array_equal(c, ref), dict(zip(ak.COUNTER_NAMES, (c[-1] - ref[-1]).tolist()))
+    yr = g["y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + g["atol"])) ** 2)))
+    assert w <= max(3.0 * float(g["omp_wrms"].max()), 1e-6) and w <= 10.0, w
