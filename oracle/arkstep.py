@@ -24,7 +24,7 @@ from . import heat_cvode as hc
 from . import port
 
 COUNTER_NAMES = ("nst", "nst_attempts", "nfi", "netf", "ncfn", "nni", "nnf", "nli", "nps",
-                 "njtimes", "nfeDQ", "ncfl", "nfe", "nnlfi", "nsetups", "nje")
+                 "njtimes", "nfeDQ", "ncfl", "nfe", "nnlfi", "nsetups", "nje", "npe")
 REAL_NAMES = ("hold", "hnext", "tcur", "h0u")
 TABLE_KEYS = ("A", "b", "c", "d", "orders")
 
@@ -67,6 +67,7 @@ def ref_lib() -> ct.CDLL:
         ("ARKodeSStolerances", I, [VP, D, D]),
         ("ARKodeSVtolerances", I, [VP, D, VP]),
         ("ARKodeSetJacFn", I, [VP, VP]),
+        ("ARKodeSetJacTimes", I, [VP, VP, VP]),
         ("ARKodeSetMaxNumSteps", I, [VP, ct.c_long]),
         ("SUNNonlinSol_Newton", VP, [VP, VP]),
         ("SUNNonlinSolFree", I, [VP]),
@@ -100,7 +101,8 @@ def ref_lib() -> ct.CDLL:
                  "ARKodeGetNumStepSolveFails", "ARKodeGetNumNonlinSolvIters",
                  "ARKodeGetNumNonlinSolvConvFails", "ARKodeGetNumLinIters",
                  "ARKodeGetNumPrecSolves", "ARKodeGetNumJtimesEvals", "ARKodeGetNumLinRhsEvals",
-                 "ARKodeGetNumLinConvFails", "ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals"):
+                 "ARKodeGetNumLinConvFails", "ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals",
+                 "ARKodeGetNumPrecEvals"):
         f = getattr(L, name)
         f.restype, f.argtypes = I, [VP, ct.POINTER(ct.c_long)]
     for name in ("ARKodeGetLastStep", "ARKodeGetCurrentStep", "ARKodeGetCurrentTime",
@@ -134,6 +136,8 @@ def port_lib() -> ct.CDLL:
         L.arkstep_port_set_matrix.argtypes = [VP, VP, VP]
         L.arkstep_port_set_vabstol.restype = None
         L.arkstep_port_set_vabstol.argtypes = [VP, D, VP]
+        L.arkstep_port_set_psetup.restype = None
+        L.arkstep_port_set_psetup.argtypes = [VP, VP]
         L._arkstep_declared = True
     return L
 
@@ -268,7 +272,6 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
     y = L.N_VNew_Serial(n, ctx) if threads is None else L.N_VNew_OpenMP(n, threads, ctx)
     prob.arr(y)[:] = u0
     f, jt, ps, pv = prob.addresses()
-    assert direct or (ps is None and jt is None)
     fe, fi = prob.imex_addresses() if imex else (None, f)
     mem = L.ERKStepCreate(f, 0.0, y, ctx) if erk else L.ARKStepCreate(fe, fi, 0.0, y, ctx)
     assert mem
@@ -305,7 +308,9 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         assert L.ARKodeSetNonlinearSolver(mem, NLS) == 0
         LS = L.SUNLinSol_SPGMR(y, 1, 0, ctx)
         assert L.ARKodeSetLinearSolver(mem, LS, None) == 0
-        assert L.ARKodeSetPreconditioner(mem, None, pv) == 0
+        if jt:
+            assert L.ARKodeSetJacTimes(mem, None, jt) == 0
+        assert L.ARKodeSetPreconditioner(mem, ps, pv) == 0
     cnt, real, sols = [], [], []
     t, c, r = D(), ct.c_long(), D()
     table = None
@@ -344,7 +349,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
         L.ARKodeGetNumRhsEvals(mem, 0, ct.byref(c))
         row.append(c.value)
         row.append(TL.nnlfi if TL else 0)
-        for name in ("ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals"):
+        for name in ("ARKodeGetNumLinSolvSetups", "ARKodeGetNumJacEvals", "ARKodeGetNumPrecEvals"):
             if LS:
                 getattr(L, name)(mem, ct.byref(c))
                 row.append(c.value)
@@ -376,7 +381,7 @@ def run_reference_with(make_serial, u0, touts, rtol, atol, order=3, mxstep=10000
 
 
 def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mxstep=100000,
-             block_solve=None, fixed_point=None, matrix=None, vatol_handle=None):
+             block_solve=None, fixed_point=None, matrix=None, vatol_handle=None, psetup=None):
     """The restated ARKStep on the objects it is given: y0_handle (an
     N_Vector holding u0, also used for the outputs), LS_handle (a
     SUNLinearSolver built on it), callbacks = (fe, fi, jtimes, psolve,
@@ -387,7 +392,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
     Newton, with LS_handle and the preconditioner None; fixed_point = m: the
     fixed-point solver with Anderson depth m, also without a linear solver;
     matrix = (SUNMatrix, ARKLsJacFn address): the matrix-based path with a
-    direct LS_handle; vatol_handle: an N_Vector of absolute tolerances."""
+    direct LS_handle; vatol_handle: an N_Vector of absolute tolerances;
+    psetup: a preconditioner setup (ARKLsPrecSetupFn address) beside psolve."""
     P = port_lib()
     fe, fi, jt, pv, data = callbacks
     DP = ct.POINTER(D)
@@ -419,6 +425,8 @@ def run_port(y0_handle, LS_handle, callbacks, get, touts, tables, rtol, atol, mx
         P.arkstep_port_set_matrix(mem, matrix[0], matrix[1])
     if vatol_handle:
         P.arkstep_port_set_vabstol(mem, rtol, vatol_handle)
+    if psetup:
+        P.arkstep_port_set_psetup(mem, psetup)
     cnt, real, sols = [], [], []
     t = D()
     cbuf = (ct.c_long * len(COUNTER_NAMES))()
@@ -456,14 +464,15 @@ def run_port_serial_with(make_serial, u0, touts, tables, rtol, atol, task_local=
     if np.ndim(atol) != 0:
         vatol = L.N_VNew_Serial(len(u0), ctx)
         prob.arr(vatol)[:] = atol
-    f, jt, _, pv = prob.addresses()
+    f, jt, ps, pv = prob.addresses()
     fe, fi = prob.imex_addresses() if tables["e"] is not None else (None, f)
     try:
         return run_port(y, LS, (fe, fi, None if direct else jt,
                                 None if (no_ls or direct) else pv, None),
                         lambda h: prob.arr(h).copy(), touts, tables, rtol, atol,
                         block_solve=prob.block_solve_address() if task_local else None,
-                        fixed_point=fixed_point, matrix=matrix, vatol_handle=vatol)
+                        fixed_point=fixed_point, matrix=matrix, vatol_handle=vatol,
+                        psetup=None if (no_ls or direct) else ps)
     finally:
         if LS:
             L.SUNLinSolFree(LS)

@@ -2,12 +2,12 @@
  *
  * ARKODE's ARKStep with an implicit right-hand side (a DIRK method) or an
  * explicit + implicit splitting (an ARK IMEX method), the Newton nonlinear
- * solver and a matrix-free iterative SUNLinearSolver (user or
- * difference-quotient Jacobian-times-vector, a preconditioner solve without a
- * preconditioner setup), the benchmark's task-local Newton, or the
- * fixed-point solver with Anderson acceleration (oracle/fixedpoint_port.c);
- * and ERKStep (explicit only) -- the ERK, ARK-DIRK and ARK-IMEX
- * configurations of the
+ * solver with a matrix-free iterative SUNLinearSolver (user or
+ * difference-quotient Jacobian-times-vector, a preconditioner solve with or
+ * without a preconditioner setup) or a matrix-based direct one (SUNMatrix,
+ * user Jacobian), the benchmark's task-local Newton, or the fixed-point
+ * solver with Anderson acceleration (oracle/fixedpoint_port.c); and ERKStep
+ * (explicit only) -- the ERK, ARK-DIRK and ARK-IMEX configurations of the
  * 3-D advection-reaction benchmark (benchmarks/advection_reaction_3D/raja/
  * arkode_driver.cpp:51-160, 239-370) -- restated over the generic object model: every
  * vector operation is dispatched through the vector's ops table (fused
@@ -47,7 +47,7 @@
  *                                  src/arkode/arkode_arkstep_nls.c:364-604, 1152-1200
  *   SUNNonlinSolSolve_Newton       src/sunnonlinsol/newton/sunnonlinsol_newton.c:179-310
  *   ARKodeSetLinearSolver defaults, arkLsInitialize, arkLsATimes,
- *   arkLsDQJtimes, arkLsPSolve, arkLsLinSys, arkLsSetup, arkLsSolve
+ *   arkLsDQJtimes, arkLsPSetup, arkLsPSolve, arkLsLinSys, arkLsSetup, arkLsSolve
  *   arkStep_NlsLSetup              arkode_arkstep_nls.c:472-512
  *                                  src/arkode/arkode_ls.c:50-300, 2319-2456, 2842-2880,
  *                                  2981-3160, 3308-3520
@@ -113,6 +113,9 @@ typedef int (*ArkJTimesFn)(N_Vector v, N_Vector Jv, double t, N_Vector y, N_Vect
                            void* user_data, N_Vector tmp);
 typedef int (*ArkPSolveFn)(double t, N_Vector y, N_Vector fy, N_Vector r, N_Vector z,
                            double gamma, double delta, int lr, void* user_data);
+/* ARKLsPrecSetupFn */
+typedef int (*ArkPSetupFn)(double t, N_Vector y, N_Vector fy, sunbooleantype jok,
+                           sunbooleantype* jcurPtr, double gamma, void* user_data);
 /* ARKLsJacFn */
 typedef int (*ArkJacFn)(double t, N_Vector y, N_Vector fy, SUNMatrix J, void* user_data,
                         N_Vector tmp1, N_Vector tmp2, N_Vector tmp3);
@@ -127,13 +130,14 @@ typedef struct
   ArkRhsFn fe, fi;
   ArkJTimesFn jtimes;
   ArkPSolveFn psolve;
+  ArkPSetupFn pset; /* set: SPGMR's preconditioner setup, through arkLsSetup */
   ArkBlockSolveFn block_lsolve; /* set: the task-local Newton, no SUNLinearSolver */
   FPPort* fp;                   /* set: the fixed-point solver, no SUNLinearSolver */
   SUNMatrix Amat, savedJ;       /* set: a matrix-based (direct) linear solver */
   ArkJacFn jac;
   N_Vector Vabstol;             /* ARKodeSVtolerances' copy, or NULL */
   int jcur, nls_jcur, jbad, convfail;
-  long nsetups, nje, nstlp, nstlj;
+  long nsetups, nje, nstlp, nstlj, npe;
   void* user_data;
   double rtol, atol;
   long mxstep;
@@ -343,6 +347,13 @@ static int ls_atimes(void* mem, N_Vector v, N_Vector z)
   return 0;
 }
 
+static int ls_psetup(void* mem)
+{ /* arkLsPSetup: jok = !jbad, jcurPtr = the step's jcur */
+  ArkPort* m = (ArkPort*)mem;
+  return m->pset(m->ls_tcur, m->ls_ycur, m->ls_fcur, !(m->jbad), &m->jcur, m->gamma,
+                 m->user_data);
+}
+
 static int ls_psolve(void* mem, N_Vector r, N_Vector z, double tol, int lr)
 { /* arkLsPSolve */
   ArkPort* m = (ArkPort*)mem;
@@ -382,6 +393,18 @@ static int ls_setup(ArkPort* m, int convfail, double tpred, N_Vector ypred, N_Ve
   const int dgamma_fail  = fabs(m->gamrat - 1.0) >= DGMAX;
   m->jbad = m->initsetup || (m->nst >= m->nstlj + ARKLS_MSBJ) ||
             ((convfail == FAIL_BAD_J) && !dgamma_fail) || (convfail == FAIL_OTHER);
+  if (!m->Amat)
+  { /* matrix-free: the preconditioner setup runs inside the LS setup */
+    m->jcur       = m->jbad;
+    int last_flag = m->LS->ops->setup(m->LS, NULL);
+    if (m->jcur)
+    {
+      m->npe++;
+      m->nstlj = m->nst;
+    }
+    if (m->jbad) m->jcur = SUNTRUE;
+    return last_flag;
+  }
   int retval = ls_linsys(m, tpred, ypred, fpred, !m->jbad);
   if (m->jcur)
   {
@@ -575,7 +598,7 @@ static int newton_solve(ArkPort* m, N_Vector zcor, double tol, int callLSetup)
       retval = nls_residual(m, zcor, delta);
       if (retval != 0) break;
     }
-    if ((retval > 0) && !m->nls_jcur && m->Amat)
+    if ((retval > 0) && !m->nls_jcur && (m->Amat || m->pset))
     {
       m->nconvfails++;
       callLSetup = 1;
@@ -612,7 +635,7 @@ static int fp_ctest(void* mem, N_Vector zcor, N_Vector del, double tol, int curi
 static int nls(ArkPort* m, int nflag)
 { /* arkStep_Nls: an lsetup exists only with a matrix-based linear solver */
   int callLSetup = 0;
-  if (m->Amat)
+  if (m->Amat || m->pset)
   {
     m->convfail = ((nflag == FIRST_CALL) || (nflag == PREV_ERR_FAIL)) ? NO_FAILURES : FAIL_OTHER;
     callLSetup = m->firststage || (fabs(m->gamrat - 1.0) > DGMAX) ||
@@ -1233,6 +1256,15 @@ void arkstep_port_set_matrix(void* mem, SUNMatrix A, ArkJacFn jac)
   if (!m->savedJ) m->savedJ = A->ops->clone(A);
 }
 
+/* ARKodeSetPreconditioner(psetup, psolve) with a preconditioner setup: the
+ * iterative solver's setup then calls it (arkLsSetup without a matrix). */
+void arkstep_port_set_psetup(void* mem, ArkPSetupFn pset)
+{
+  ArkPort* m = (ArkPort*)mem;
+  m->pset    = pset;
+  if (m->LS->ops->setpreconditioner) m->LS->ops->setpreconditioner(m->LS, m, ls_psetup, ls_psolve);
+}
+
 /* ARKodeSVtolerances(rtol, abstol): a copy of abstol (all entries > 0). */
 void arkstep_port_set_vabstol(void* mem, double rtol, N_Vector abstol)
 {
@@ -1355,7 +1387,7 @@ int arkstep_port_solve(void* mem, double tout, N_Vector yout, double* tret)
 }
 
 /* counters: nst, nst_attempts, nfi, netf, ncfn, nni, nnf, nli, nps, njtimes,
- * nfeDQ, ncfl, nfe, nnlfi, nsetups, nje; reals: last step, next step, current time, first step */
+ * nfeDQ, ncfl, nfe, nnlfi, nsetups, nje, npe; reals: last step, next step, current time, first step */
 void arkstep_port_stats(void* mem, long* cnt, double* r)
 {
   ArkPort* m = (ArkPort*)mem;
@@ -1375,6 +1407,7 @@ void arkstep_port_stats(void* mem, long* cnt, double* r)
   cnt[13]    = m->nnlfi;
   cnt[14]    = m->nsetups;
   cnt[15]    = m->nje;
+  cnt[16]    = m->npe;
   r[0]       = m->hold;
   r[1]       = m->next_h;
   r[2]       = m->tcur;

@@ -241,3 +241,22 @@ def run_port_serial_arkode_direct(ncells: int, tables, touts=TOUTS, rtol=1e-4, a
     atol = vector_atol(ncells) if atol is None else atol
     return ak.run_port_serial_with(lambda L: SerialRobertson(L, k), initial(ncells), touts,
                                    tables, rtol, atol, direct=True)
+
+
+def run_reference_arkode(ncells: int, touts=TOUTS, rtol=1e-4, atol=None, threads=None):
+    """ARKStep (DIRK, order 3, Newton) with SPGMR (left, maxl 5), the user J v
+    and the exact block-Jacobi preconditioner with its setup
+    (ARKodeSetPreconditioner(psetup, psolve)): the iterative path of ARKLS."""
+    from . import arkstep as ak
+    k = rates(ncells)
+    atol = vector_atol(ncells) if atol is None else atol
+    return ak.run_reference_with(lambda L: SerialRobertson(L, k), initial(ncells), touts, rtol,
+                                 atol, threads=threads)
+
+
+def run_port_serial_arkode(ncells: int, tables, touts=TOUTS, rtol=1e-4, atol=None):
+    from . import arkstep as ak
+    k = rates(ncells)
+    atol = vector_atol(ncells) if atol is None else atol
+    return ak.run_port_serial_with(lambda L: SerialRobertson(L, k), initial(ncells), touts,
+                                   tables, rtol, atol)

@@ -166,3 +166,38 @@ def test_arkstep_robertson_direct_block_lu_matches_reference(fma):
     yr = g["y_last"]
     w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + g["atol"])) ** 2)))
     assert w <= max(3.0 * float(g["omp_wrms"].max()), 1e-6) and w <= 10.0, w
+
+
+@pytest.mark.parametrize("fused", [False, True], ids=["unfused_gs", "fused_gs"])
+@pytest.mark.parametrize("fma", [False, True], ids=["exact", "fma"])
+def test_arkstep_robertson_preconditioned_matches_reference(fma, fused):
+    """The same cells through ARKStep with SPGMR_GB300 (left, maxl 5), the
+    device J v and the exact block-Jacobi preconditioner with its setup
+    (ARKodeSetPreconditioner(psetup, psolve), the block LU inside): every
+    counter after every output equal to the reference's (its own
+    reduction-order runs never moved one), the last solution within 3x its
+    own weighted RMS deviation and 10 tolerances."""
+    from sundials_gb300.nvector import NVector
+    from sundials_gb300.robertson import LU_FP64, Robertson
+    from sundials_gb300.spgmr import PREC_LEFT, SPGMR
+    g = np.load(ROB_GOLDEN)
+    rtol = float(g["rtol"])
+    y = NVector.from_numpy(g["u0"])
+    y.set_fma(fma)
+    vatol = NVector.from_numpy(g["atol"])
+    prob = Robertson(g["k"], y, LU_FP64)
+    S = SPGMR(y, pretype=PREC_LEFT, maxl=5)
+    assert S.set_fused(fused) == 0
+    try:
+        f, jt, ps, pv, data = prob.cvode_callbacks()
+        c, r, s = ak.run_port(y.v, S.S, (None, f, jt, pv, data), lambda h: y.get(),
+                              [float(t) for t in g["touts"]], ak.tables_from(g, "prec_"), rtol,
+                              0.0, vatol_handle=vatol.v, psetup=ps)
+    finally:
+        S.free()
+        prob.free()
+    ref = g["prec_counters"]
+    assert np.array_equal(c, ref), dict(zip(ak.COUNTER_NAMES, (c[-1] - ref[-1]).tolist()))
+    yr = g["prec_y_last"]
+    w = float(np.sqrt(np.mean(((s[-1] - yr) / (rtol * np.abs(yr) + g["atol"])) ** 2)))
+    assert w <= max(3.0 * float(g["prec_omp_wrms"].max()), 1e-6) and w <= 10.0, w

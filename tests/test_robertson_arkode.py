@@ -53,3 +53,29 @@ def test_golden_reproduced():
     assert np.array_equal(c, g["counters"])
     assert np.array_equal(r.view(np.int64), g["reals"].view(np.int64))
     assert np.array_equal(s[-1].view(np.int64), g["y_last"].view(np.int64))
+
+
+@needs_ref
+@pytest.mark.parametrize("ncells,nout", [(16, 12), (24, 7)])
+def test_preconditioned_path_bit_identical_to_reference(ncells, nout):
+    """ARKLS's iterative path with a preconditioner setup (arkLsSetup without
+    a matrix, arkLsPSetup's jok / jcur logic): SPGMR with the user J v and
+    the exact block-Jacobi preconditioner."""
+    touts = rc.TOUTS[:nout]
+    c_ref, r_ref, s_ref, tables = rc.run_reference_arkode(ncells, touts=touts)
+    c_p, r_p, s_p = rc.run_port_serial_arkode(ncells, tables, touts=touts)
+    assert np.array_equal(c_p, c_ref), (c_p[-1] - c_ref[-1]).tolist()
+    assert np.array_equal(r_p.view(np.int64), r_ref.view(np.int64))
+    assert np.array_equal(s_p.view(np.int64), s_ref.view(np.int64))
+    last = dict(zip(ak.COUNTER_NAMES, c_ref[-1]))
+    assert last["npe"] > 0 and last["nli"] > 0 and last["ncfl"] > 0
+
+
+@needs_ref
+def test_preconditioned_golden_reproduced():
+    g = np.load(GOLDEN)
+    c, r, s = rc.run_port_serial_arkode(int(g["cells"]), ak.tables_from(g, "prec_"),
+                                        touts=[float(t) for t in g["touts"]])
+    assert np.array_equal(c, g["prec_counters"])
+    assert np.array_equal(r.view(np.int64), g["prec_reals"].view(np.int64))
+    assert np.array_equal(s[-1].view(np.int64), g["prec_y_last"].view(np.int64))
