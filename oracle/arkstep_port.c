@@ -537,9 +537,6 @@ static int nls_convtest(ArkPort* m, N_Vector del, double tol, int mcur)
   return NLS_CONTINUE;
 }
 
-/* SUNNonlinSolSolve_Newton without a linear solver setup function (the
- * matrix-free solver with no preconditioner setup disables it), so a
- * recoverable failure is never retried with a fresh setup. */
 /* arkStep_NlsLSetup (arkode_arkstep_nls.c:472-512) */
 static int nls_lsetup(ArkPort* m, int jbad)
 {
@@ -556,9 +553,9 @@ static int nls_lsetup(ArkPort* m, int jbad)
   return 0;
 }
 
-/* SUNNonlinSolSolve_Newton; a recoverable failure is retried once with a
- * fresh setup (jbad) when there is a linear solver setup (a matrix) and the
- * Jacobian was not current */
+/* SUNNonlinSolSolve_Newton; a recoverable failure is retried with a fresh
+ * setup (jbad) when there is a linear solver setup (a matrix or a
+ * preconditioner setup) and the Jacobian was not current */
 static int newton_solve(ArkPort* m, N_Vector zcor, double tol, int callLSetup)
 {
   N_Vector delta = m->delta;
@@ -633,7 +630,8 @@ static int fp_ctest(void* mem, N_Vector zcor, N_Vector del, double tol, int curi
 }
 
 static int nls(ArkPort* m, int nflag)
-{ /* arkStep_Nls: an lsetup exists only with a matrix-based linear solver */
+{ /* arkStep_Nls: an lsetup exists with a matrix-based linear solver or a
+   * preconditioner setup (arkLsInitialize disables it otherwise) */
   int callLSetup = 0;
   if (m->Amat || m->pset)
   {
