@@ -3,8 +3,10 @@
  * Robertson chemical-kinetics cells (3 species each, y1 y2 y3 of cell c at
  * 3c, 3c+1, 3c+2 of one NVECTOR_GB300 vector), with per-cell rate constants:
  *   y1' = -k1 y1 + k3 y2 y3,   y3' = k2 y2^2,   y2' = -y1' - y3'.
- * These are the callbacks a CVODE + SPGMR run of the batch needs --
- * right-hand side, Jacobian-times-vector, and the exact block-Jacobi
+ * These are the callbacks a CVODE or ARKODE (ARKStep, implicit right-hand
+ * side) + SPGMR run of the batch needs (the two packages' callback types
+ * have the same signatures): right-hand side, Jacobian-times-vector, and
+ * the exact block-Jacobi
  * preconditioner P = I - gamma J_c per cell, factored and applied by
  * SUNLinSol_BlockLU_GB300 on a SUNMatrix_BlockDiag_GB300 of 3x3 blocks.
  *
@@ -39,18 +41,20 @@ SUNGB300_EXPORT SUNRoberts_GB300 SUNRoberts_GB300_Create(sunindextype ncells,
                                                          int lu_precision, SUNContext sunctx);
 SUNGB300_EXPORT void SUNRoberts_GB300_Free(SUNRoberts_GB300 p);
 
-/* CVRhsFn */
+/* CVRhsFn / ARKRhsFn */
 SUNGB300_EXPORT int SUNRoberts_GB300_RHS(sunrealtype t, N_Vector y, N_Vector ydot, void* p);
-/* CVLsJacTimesVecFn: Jv = J(y) v */
+/* CVLsJacTimesVecFn / ARKLsJacTimesVecFn: Jv = J(y) v */
 SUNGB300_EXPORT int SUNRoberts_GB300_JTimes(N_Vector v, N_Vector Jv, sunrealtype t, N_Vector y,
                                             N_Vector fy, void* p, N_Vector tmp);
-/* CVLsJacFn: J(y) into a SUNMatrix_BlockDiag_GB300 of ncells 3x3 blocks, for
- * CVodeSetLinearSolver(cvode_mem, SUNLinSol_BlockLU_GB300(y, J, ...), J) +
- * CVodeSetJacFn -- the reference example's direct block solve
+/* CVLsJacFn / ARKLsJacFn: J(y) into a SUNMatrix_BlockDiag_GB300 of ncells
+ * 3x3 blocks, for CVodeSetLinearSolver(cvode_mem, SUNLinSol_BlockLU_GB300(y,
+ * J, ...), J) + CVodeSetJacFn (or the ARKode* equivalents) -- the reference
+ * example's direct block solve
  * (cvRoberts_block_cusolversp_batchqr.cu:196-223, there on cuSolverSp). */
 SUNGB300_EXPORT int SUNRoberts_GB300_Jac(sunrealtype t, N_Vector y, N_Vector fy, SUNMatrix J,
                                          void* p, N_Vector tmp1, N_Vector tmp2, N_Vector tmp3);
-/* CVLsPrecSetupFn / CVLsPrecSolveFn: exact block-Jacobi preconditioner.
+/* CVLsPrecSetupFn / CVLsPrecSolveFn (ARKLsPrecSetupFn / ARKLsPrecSolveFn):
+ * exact block-Jacobi preconditioner.
  * Setup returns 1 (recoverable) if a block is singular. */
 SUNGB300_EXPORT int SUNRoberts_GB300_CVPSetup(sunrealtype t, N_Vector y, N_Vector fy,
                                               sunbooleantype jok, sunbooleantype* jcurPtr,
