@@ -95,6 +95,9 @@ void fp_port_free(FPPort* fp)
   free(fp);
 }
 
+/* SUNNonlinSolSetMaxIters_FixedPoint (the integrators keep the default 3) */
+void fp_port_set_maxiters(FPPort* fp, int maxiters) { fp->maxiters = maxiters; }
+
 long fp_port_niters(const FPPort* fp) { return fp->niters; }
 long fp_port_nconvfails(const FPPort* fp) { return fp->nconvfails; }
 

@@ -15,6 +15,7 @@ FPPort* fp_port_create(N_Vector tmpl, int m); /* maxiters 3, no damping */
 void fp_port_free(FPPort* fp);
 int fp_port_solve(FPPort* fp, N_Vector ycor, double tol, FPSysFn sys, FPCTestFn ctest,
                   void* mem);
+void fp_port_set_maxiters(FPPort* fp, int maxiters);
 long fp_port_niters(const FPPort* fp);
 long fp_port_nconvfails(const FPPort* fp);
 
