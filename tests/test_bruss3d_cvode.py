@@ -101,7 +101,8 @@ def test_fixed_point_golden_reproduced():
 @pytest.mark.parametrize("shape,c,tf,k,rtol", [
     ((6, 5, 7), -0.02, 0.01, None, 1e-6),                 # the benchmark's stiff reaction
     ((6, 5, 7), -0.02, 10.0, (1, 1, 1, 1, 1, 1), 1e-10),  # non-stiff: orders up to 7
-    ((5, 6, 4), 0.02, 5.0, (1, 1, 1, 1, 2, 2), 1e-12)])
+    ((5, 6, 4), 0.02, 5.0, (1, 1, 1, 1, 2, 2), 1e-12),
+    ((4, 4, 4), 0.001, 10.0, (0.1, 0.1, 0.1, 0.1, 0.1, 0.1), 1e-14)])  # order 8
 def test_adams_restatement_is_the_reference_cvode(shape, c, tf, k, rtol):
     """cvode_driver.cpp's CV-ADAMS configuration (Adams-Moulton with the
     fixed-point solver): the restatement bit for bit, including orders above
